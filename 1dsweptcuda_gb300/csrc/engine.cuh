@@ -1,0 +1,368 @@
+// Kernels of the swept and classic schemes, generic over the problem P
+// (SW_HEAT / SW_KS / SW_EULER) and the precision T.  Each k_*.cu includes this
+// file and instantiates one problem for float and double.
+//
+// Swept decomposition (the reference's upTriangle / wholeDiamond /
+// splitDiamond / downTriangle, Heat1D_SweptShared.cu:147-408,
+// KS1D_SweptShared.cu:209-394, Euler1D_SweptShared.cu:437-746), laid out for
+// GB300:
+//  * a tile of W cells keeps two rows in shared memory; sub-step m reads row
+//    (m-1)&1 and writes row m&1 (Heat: the two time-parity rows; KS/Euler: row
+//    0 = u, row 1 = predictor u*, the corrector adds into row 0).  Each row has
+//    R margin cells on both sides;
+//  * the up part computes sub-steps u = 1..H-1 (H = W/(2R)) on [uR, W-uR); the
+//    down part of a tile shifted by W/2 computes j = 1..H on [W/2-jR, W/2+jR);
+//  * the edge exchange goes through one slot of W cells per half-tile
+//    (2*nx cells in all): row 0 of the half, then row 1 of the half moved R
+//    cells toward the tile centre.  A diamond reads the slots of its two halves
+//    and overwrites the same two slots with its own exports, so one buffer
+//    serves every pass (no ping-pong) and each access is a contiguous,
+//    coalesced run of W/2 cells;
+//  * phase 0 tiles start at t*W, phase 1 tiles at t*W + W/2 (mod nx), so the
+//    reference's "split" diamond is simply the last phase-1 tile, whose
+//    positions wrap; boundary conditions are applied per cell from its global
+//    position.
+// Every (cell, sub-step) value is computed once with the classic arithmetic,
+// so swept, variant and classic agree bit for bit.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <type_traits>
+
+#include "stencils.cuh"
+#include "sw_internal.h"
+
+namespace sw {
+
+template <typename T>
+struct alignas(4 * sizeof(T)) V4 {
+    T x, y, z, w;
+};
+
+template <int P, typename T>
+struct Scheme {
+    static constexpr int R = (P == SW_HEAT) ? 1 : 2;
+    static constexpr int S = (P == SW_HEAT) ? 1 : 2;
+    static constexpr int C = (P == SW_EULER) ? 3 : 1;
+    // threads per block: one per cell for Heat/KS; Euler caps at 256 so its
+    // long stencil keeps its registers (a thread then walks W/256 cells)
+    static constexpr int MAXT = (P == SW_EULER) ? 256 : 1024;
+    using G = typename std::conditional<P == SW_EULER, V4<T>, T>::type;
+};
+
+// ---- shared-memory tile access: layout [row][component][L], L = W + 2R
+template <int P, typename T>
+__device__ __forceinline__ void tile_put(T *rows, int L, int row, int x, const typename Scheme<P, T>::G &v) {
+    constexpr int R = Scheme<P, T>::R;
+    if constexpr (P == SW_EULER) {
+        T *b = rows + row * 3 * L + R + x;
+        b[0] = v.x;
+        b[L] = v.y;
+        b[2 * L] = v.z;
+    } else {
+        rows[row * L + R + x] = v;
+    }
+}
+template <int P, typename T>
+__device__ __forceinline__ typename Scheme<P, T>::G tile_get(const T *rows, int L, int row, int x) {
+    constexpr int R = Scheme<P, T>::R;
+    if constexpr (P == SW_EULER) {
+        const T *b = rows + row * 3 * L + R + x;
+        return V4<T>{b[0], b[L], b[2 * L], T(0)};
+    } else {
+        return rows[row * L + R + x];
+    }
+}
+
+// One sub-step of parity `par` (1: predictor / odd Heat step; 0: corrector /
+// even Heat step) at tile cell x, global position gp.
+template <int P, typename T>
+__device__ __forceinline__ void tile_point(const Params<T> &p, T *rows, int L, int par, int x, int64_t gp) {
+    constexpr int R = Scheme<P, T>::R;
+    constexpr int C = Scheme<P, T>::C;
+    const T *src = rows + (par ^ 1) * C * L + R;
+    T *dst = rows + par * C * L + R;
+    if constexpr (P == SW_HEAT) {
+        int l = x - 1, r = x + 1;
+        if (p.bc != SW_BC_PERIODIC) {  // insulated ends, Heat1D_SweptShared.cu:140-142,352-353
+            if (gp == 0) l = x + 1;
+            if (gp == p.nx - 1) r = x - 1;
+        }
+        dst[x] = heat_step(p, src[l], src[x], src[r]);
+    } else if constexpr (P == SW_KS) {
+        if (par)
+            dst[x] = ks_predict(p, src[x - 2], src[x - 1], src[x], src[x + 1], src[x + 2]);
+        else
+            dst[x] = ks_correct(p, dst[x], src[x - 2], src[x - 1], src[x], src[x + 1], src[x + 2]);
+    } else {
+        if (gp == 0 || gp == p.nx - 1) return;  // Dirichlet cells, Euler1D_SweptShared.cu:405-416
+        const bool fl = (gp == 1), fr = (gp == p.nx - 2);
+        Q3<T> s[5];
+#pragma unroll
+        for (int k = 0; k < 5; ++k) s[k] = q3(src[x - 2 + k], src[L + x - 2 + k], src[2 * L + x - 2 + k]);
+        Q3<T> o;
+        if (par) {
+            o = eu_predict(p, s, fl, fr);
+        } else {
+            o = eu_correct(p, q3(dst[x], dst[L + x], dst[2 * L + x]), s, fl, fr);
+        }
+        dst[x] = o.x;
+        dst[L + x] = o.y;
+        dst[2 * L + x] = o.z;
+    }
+}
+
+template <int P, typename T>
+__host__ __device__ constexpr size_t swept_smem_bytes(int W) {
+    return sizeof(T) * 2 * Scheme<P, T>::C * (size_t)(W + 2 * Scheme<P, T>::R);
+}
+
+__device__ __forceinline__ int64_t wrap_pos(int64_t q, int64_t nx) {
+    if (q >= nx) q -= nx;
+    if (q < 0) q += nx;
+    return q;
+}
+
+// Euler: both rows of the Dirichlet cells hold the boundary states
+// (splitDiamond, Euler1D_SweptShared.cu:684-694).
+template <int P, typename T>
+__device__ __forceinline__ void tile_fix_bc(const Params<T> &p, T *rows, int L, int64_t base) {
+    if constexpr (P == SW_EULER) {
+        constexpr int R = Scheme<P, T>::R;
+        for (int i = threadIdx.x; i < L; i += blockDim.x) {
+            const int x = i - R;
+            const int64_t gp = wrap_pos(base + x, p.nx);
+            if (gp == 0 || gp == p.nx - 1) {
+                const int side = (gp == 0) ? 0 : 1;
+                V4<T> b{p.bd[3 * side], p.bd[3 * side + 1], p.bd[3 * side + 2], T(0)};
+                tile_put<P, T>(rows, L, 0, x, b);
+                tile_put<P, T>(rows, L, 1, x, b);
+            }
+        }
+    }
+}
+
+// Slot layout of half-tile h: cells [h*W, h*W + W/2) = row 0, [h*W + W/2, (h+1)*W) = row 1.
+template <int P, typename T>
+__device__ __forceinline__ void tile_import(T *rows, int L, int W, const typename Scheme<P, T>::G *sl,
+                                            const typename Scheme<P, T>::G *sr) {
+    constexpr int R = Scheme<P, T>::R;
+    const int h = W >> 1;
+    for (int i = threadIdx.x; i < W; i += blockDim.x) {
+        if (i < h) {
+            tile_put<P, T>(rows, L, 0, i, sl[i]);
+            tile_put<P, T>(rows, L, 1, i - R, sl[h + i]);
+        } else {
+            const int j = i - h;
+            tile_put<P, T>(rows, L, 0, h + j, sr[j]);
+            tile_put<P, T>(rows, L, 1, h + R + j, sr[h + j]);
+        }
+    }
+}
+template <int P, typename T>
+__device__ __forceinline__ void tile_export(const T *rows, int L, int W, typename Scheme<P, T>::G *sl,
+                                            typename Scheme<P, T>::G *sr) {
+    constexpr int R = Scheme<P, T>::R;
+    const int h = W >> 1;
+    for (int i = threadIdx.x; i < W; i += blockDim.x) {
+        if (i < h) {
+            sl[i] = tile_get<P, T>(rows, L, 0, i);
+            sl[h + i] = tile_get<P, T>(rows, L, 1, R + i);
+        } else {
+            const int j = i - h;
+            sr[j] = tile_get<P, T>(rows, L, 0, h + j);
+            sr[h + j] = tile_get<P, T>(rows, L, 1, h - R + j);
+        }
+    }
+}
+
+// Down part: sub-steps j = 1..H on the growing centre [W/2 - jR, W/2 + jR).
+template <int P, typename T>
+__device__ __forceinline__ void tile_down(const Params<T> &p, T *rows, int L, int W, int64_t base) {
+    constexpr int R = Scheme<P, T>::R;
+    const int h = W >> 1, H = W / (2 * R);
+    for (int j = 1; j <= H; ++j) {
+        for (int x = threadIdx.x; x < W; x += blockDim.x)
+            if (x >= h - j * R && x < h + j * R) tile_point<P, T>(p, rows, L, j & 1, x, wrap_pos(base + x, p.nx));
+        __syncthreads();
+    }
+}
+// Up part: sub-steps u = 1..H-1 on the shrinking [uR, W - uR).
+template <int P, typename T>
+__device__ __forceinline__ void tile_up(const Params<T> &p, T *rows, int L, int W, int64_t base) {
+    constexpr int R = Scheme<P, T>::R;
+    const int H = W / (2 * R);
+    for (int u = 1; u < H; ++u) {
+        for (int x = threadIdx.x; x < W; x += blockDim.x)
+            if (x >= u * R && x < W - u * R) tile_point<P, T>(p, rows, L, u & 1, x, wrap_pos(base + x, p.nx));
+        __syncthreads();
+    }
+}
+
+// One swept pass over all tiles.  MODE_UP: state -> up-triangle -> slots
+// (phase 0 only).  MODE_DIAMOND: slots -> down + up -> slots.  MODE_DOWN:
+// slots -> down-triangle -> state.  Block = one tile.
+template <int P, typename T, int MODE>
+__global__ void __launch_bounds__(Scheme<P, T>::MAXT) k_swept(const Params<T> p, typename Scheme<P, T>::G *__restrict__ state,
+                                                typename Scheme<P, T>::G *__restrict__ slots, const int W,
+                                                const int phase) {
+    using G = typename Scheme<P, T>::G;
+    constexpr int R = Scheme<P, T>::R;
+    extern __shared__ __align__(16) unsigned char sw_smem[];
+    T *rows = reinterpret_cast<T *>(sw_smem);
+    const int L = W + 2 * R, h = W >> 1;
+    const int64_t nx = p.nx, nhalf = nx / h, t = blockIdx.x;
+    const int64_t base = t * W + (int64_t)phase * h;
+    const int64_t hl = (2 * t + phase) % nhalf;
+    const int64_t hr = (hl + 1 == nhalf) ? 0 : hl + 1;
+
+    if constexpr (MODE == MODE_UP) {
+        for (int x = threadIdx.x; x < W; x += blockDim.x) tile_put<P, T>(rows, L, 0, x, state[base + x]);
+    } else {
+        tile_import<P, T>(rows, L, W, slots + hl * W, slots + hr * W);
+    }
+    if constexpr (P == SW_EULER) {
+        __syncthreads();
+        tile_fix_bc<P, T>(p, rows, L, base);
+    }
+    __syncthreads();
+    if constexpr (MODE != MODE_UP) tile_down<P, T>(p, rows, L, W, base);
+    if constexpr (MODE == MODE_DOWN) {
+        for (int x = threadIdx.x; x < W; x += blockDim.x) state[wrap_pos(base + x, nx)] = tile_get<P, T>(rows, L, 0, x);
+    } else {
+        tile_up<P, T>(p, rows, L, W, base);
+        tile_export<P, T>(rows, L, W, slots + hl * W, slots + hr * W);
+    }
+}
+
+// One classic sub-step over all cells: classicHeat (Heat1D_SweptShared.cu:132-145),
+// classicKS (KS1D_SweptShared.cu:189-207), classicEuler (Euler1D_SweptShared.cu:400-426).
+template <int P, typename T>
+__global__ void __launch_bounds__(Scheme<P, T>::MAXT) k_classic(const Params<T> p, const typename Scheme<P, T>::G *__restrict__ in,
+                                                  typename Scheme<P, T>::G *__restrict__ out, const int sub) {
+    const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t nx = p.nx;
+    if (g >= nx) return;
+    if constexpr (P == SW_HEAT) {
+        int64_t l = g - 1, r = g + 1;
+        if (p.bc == SW_BC_PERIODIC) {
+            if (l < 0) l = nx - 1;
+            if (r == nx) r = 0;
+        } else {
+            if (g == 0) l = 1;
+            if (g == nx - 1) r = nx - 2;
+        }
+        out[g] = heat_step(p, in[l], in[g], in[r]);
+    } else if constexpr (P == SW_KS) {
+        int64_t i[5];
+#pragma unroll
+        for (int k = 0; k < 5; ++k) i[k] = wrap_pos(g - 2 + k, nx);
+        if (sub == 0)
+            out[g] = ks_predict(p, in[i[0]], in[i[1]], in[i[2]], in[i[3]], in[i[4]]);
+        else
+            out[g] = ks_correct(p, out[g], in[i[0]], in[i[1]], in[i[2]], in[i[3]], in[i[4]]);
+    } else {
+        if (g == 0 || g == nx - 1) {
+            const int side = (g == 0) ? 0 : 1;
+            out[g] = V4<T>{p.bd[3 * side], p.bd[3 * side + 1], p.bd[3 * side + 2], T(0)};
+            return;
+        }
+        Q3<T> s[5];
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+            int64_t q = g - 2 + k;
+            q = q < 0 ? 0 : (q >= nx ? nx - 1 : q);  // only read when the edge flags let them matter
+            const V4<T> v = in[q];
+            s[k] = q3(v.x, v.y, v.z);
+        }
+        const bool fl = (g == 1), fr = (g == nx - 2);
+        Q3<T> o;
+        if (sub == 0) {
+            o = eu_predict(p, s, fl, fr);
+        } else {
+            const V4<T> u = out[g];
+            o = eu_correct(p, q3(u.x, u.y, u.z), s, fl, fr);
+        }
+        out[g] = V4<T>{o.x, o.y, o.z, T(0)};
+    }
+}
+
+// Euler host layout (rho, rho u, E) <-> device layout (rho, rho u, E, 0).
+template <typename T>
+__global__ void k_pack3(const T *__restrict__ in3, V4<T> *__restrict__ out4, int64_t nx) {
+    const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g < nx) out4[g] = V4<T>{in3[3 * g], in3[3 * g + 1], in3[3 * g + 2], T(0)};
+}
+template <typename T>
+__global__ void k_unpack3(const V4<T> *__restrict__ in4, T *__restrict__ out3, int64_t nx) {
+    const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g < nx) {
+        const V4<T> v = in4[g];
+        out3[3 * g] = v.x;
+        out3[3 * g + 1] = v.y;
+        out3[3 * g + 2] = v.z;
+    }
+}
+
+// ------------------------------------------------------------- launchers
+template <typename K>
+inline void allow_big_smem(K kernel) {
+    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+}
+
+template <int P, typename T>
+cudaError_t launch_classic(const void *vp, const void *in, void *out, int sub, int64_t nx, int block,
+                           cudaStream_t s) {
+    using G = typename Scheme<P, T>::G;
+    const Params<T> &p = *static_cast<const Params<T> *>(vp);
+    if (block <= 0 || block > Scheme<P, T>::MAXT) block = block <= 0 ? 256 : Scheme<P, T>::MAXT;
+    const int64_t grid = (nx + block - 1) / block;
+    k_classic<P, T><<<(unsigned)grid, block, 0, s>>>(p, static_cast<const G *>(in), static_cast<G *>(out), sub);
+    return cudaGetLastError();
+}
+
+template <int P, typename T>
+cudaError_t launch_swept(const void *vp, int mode, int phase, void *state, void *slots, int64_t nx, int W,
+                         cudaStream_t s) {
+    using G = typename Scheme<P, T>::G;
+    static bool configured = false;
+    if (!configured) {
+        allow_big_smem(k_swept<P, T, MODE_UP>);
+        allow_big_smem(k_swept<P, T, MODE_DIAMOND>);
+        allow_big_smem(k_swept<P, T, MODE_DOWN>);
+        configured = true;
+    }
+    const Params<T> &p = *static_cast<const Params<T> *>(vp);
+    const size_t smem = swept_smem_bytes<P, T>(W);
+    const unsigned grid = (unsigned)(nx / W);
+    const int threads = W < Scheme<P, T>::MAXT ? W : Scheme<P, T>::MAXT;
+    G *st = static_cast<G *>(state), *sl = static_cast<G *>(slots);
+    switch (mode) {
+    case MODE_UP: k_swept<P, T, MODE_UP><<<grid, threads, smem, s>>>(p, st, sl, W, phase); break;
+    case MODE_DIAMOND: k_swept<P, T, MODE_DIAMOND><<<grid, threads, smem, s>>>(p, st, sl, W, phase); break;
+    default: k_swept<P, T, MODE_DOWN><<<grid, threads, smem, s>>>(p, st, sl, W, phase); break;
+    }
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_pack(const void *in3, void *out4, int64_t nx, cudaStream_t s) {
+    k_pack3<T><<<(unsigned)((nx + 255) / 256), 256, 0, s>>>(static_cast<const T *>(in3), static_cast<V4<T> *>(out4),
+                                                               nx);
+    return cudaGetLastError();
+}
+template <typename T>
+cudaError_t launch_unpack(const void *in4, void *out3, int64_t nx, cudaStream_t s) {
+    k_unpack3<T><<<(unsigned)((nx + 255) / 256), 256, 0, s>>>(static_cast<const V4<T> *>(in4), static_cast<T *>(out3),
+                                                                 nx);
+    return cudaGetLastError();
+}
+
+template <int P, typename T>
+size_t smem_of(int W) {
+    return swept_smem_bytes<P, T>(W);
+}
+
+}  // namespace sw

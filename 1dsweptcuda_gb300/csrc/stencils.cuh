@@ -1,0 +1,157 @@
+// Stencil arithmetic of the three schemes, device side.
+//
+// Each function keeps the operation order of the reference's expression it
+// restates and spells every operation with a round-to-nearest intrinsic, so
+// the compiler can neither fuse nor reorder: the results are bit-identical to
+// the reference's host-compiled stencil code and to the oracle, whatever
+// -fmad setting a build uses.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "sw_internal.h"
+
+namespace sw {
+
+// ---- correctly rounded scalar operations, both precisions
+__device__ __forceinline__ double ad(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float ad(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double sb(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ float sb(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double ml(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float ml(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double dv(double a, double b) { return __ddiv_rn(a, b); }
+__device__ __forceinline__ float dv(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ double sq(double a) { return __dsqrt_rn(a); }
+__device__ __forceinline__ float sq(float a) { return __fsqrt_rn(a); }
+__device__ __forceinline__ double mn(double a, double b) { return fmin(a, b); }
+__device__ __forceinline__ float mn(float a, float b) { return fminf(a, b); }
+__device__ __forceinline__ double ab(double a) { return fabs(a); }
+__device__ __forceinline__ float ab(float a) { return fabsf(a); }
+
+// ---------------------------------------------------------------- Heat
+// execFunc, Heat1D_SweptShared.cu:121-130: fourier*(T[l] + T[r]) + fourierTwo*T[c]
+template <typename T>
+__device__ __forceinline__ T heat_step(const Params<T> &p, T l, T c, T r) {
+    return ad(ml(p.fo, ad(l, r)), ml(p.fo2, c));
+}
+
+// ------------------------------------------------------------------ KS
+// convect + secondDer + fourthDer (reciprocal build), KS1D_SweptShared.cu:136-155
+template <typename T>
+__device__ __forceinline__ T ks_rhs(const Params<T> &p, T ll, T l, T c, T r, T rr) {
+    const T two = T(2), four = T(4), six = T(6);
+    T conv = ml(sb(ml(r, r), ml(l, l)), p.c4);
+    T sec = ml(sb(ad(l, r), ml(two, c)), p.d2);
+    T fourth = ml(ad(sb(ad(sb(ll, ml(four, l)), ml(six, c)), ml(four, r)), rr), p.d4);
+    return ad(ad(conv, sec), fourth);
+}
+// stutterStep, KS1D_SweptShared.cu:159-164: u - dt/2 * rhs
+template <typename T>
+__device__ __forceinline__ T ks_predict(const Params<T> &p, T ll, T l, T c, T r, T rr) {
+    return sb(c, ml(p.dth, ks_rhs(p, ll, l, c, r, rr)));
+}
+// finalStep, KS1D_SweptShared.cu:166-171 added to u (classicKS :201-202): u + (-dt * rhs)
+template <typename T>
+__device__ __forceinline__ T ks_correct(const Params<T> &p, T u, T ll, T l, T c, T r, T rr) {
+    return ad(u, ml(-p.dt, ks_rhs(p, ll, l, c, r, rr)));
+}
+
+// --------------------------------------------------------------- Euler
+template <typename T>
+struct Q3 {
+    T x, y, z;
+};
+template <typename T>
+__device__ __forceinline__ Q3<T> q3(T x, T y, T z) { return Q3<T>{x, y, z}; }
+template <typename T>
+__device__ __forceinline__ Q3<T> qadd(Q3<T> a, Q3<T> b) { return q3(ad(a.x, b.x), ad(a.y, b.y), ad(a.z, b.z)); }
+template <typename T>
+__device__ __forceinline__ Q3<T> qsub(Q3<T> a, Q3<T> b) { return q3(sb(a.x, b.x), sb(a.y, b.y), sb(a.z, b.z)); }
+template <typename T>
+__device__ __forceinline__ Q3<T> qscale(T s, Q3<T> a) { return q3(ml(s, a.x), ml(s, a.y), ml(s, a.z)); }
+
+// pressure, Euler1D_SweptShared.cu:183-193: mgam*(E - (0.5*m*m/rho))
+template <typename T>
+__device__ __forceinline__ T eu_pressure(const Params<T> &p, Q3<T> q) {
+    return ml(p.mgam, sb(q.z, dv(ml(ml(T(0.5), q.y), q.y), q.x)));
+}
+// pressureHalf, :202-212: mgam*(z - 0.5*y*y)
+template <typename T>
+__device__ __forceinline__ T eu_pressure_half(const Params<T> &p, Q3<T> q) {
+    return ml(p.mgam, sb(q.z, ml(ml(T(0.5), q.y), q.y)));
+}
+// limitor, :222-228: cur + 0.5*min(ratio,1)*(oth - cur)
+template <typename T>
+__device__ __forceinline__ Q3<T> eu_limit(Q3<T> cur, Q3<T> oth, T ratio) {
+    return qadd(cur, qscale(ml(T(0.5), mn(ratio, T(1))), qsub(oth, cur)));
+}
+// eulerFlux, :237-257
+template <typename T>
+__device__ __forceinline__ Q3<T> eu_flux(const Params<T> &p, Q3<T> L, Q3<T> R) {
+    T uL = dv(L.y, L.x);
+    T uR = dv(R.y, R.x);
+    T pL = eu_pressure(p, L);
+    T pR = eu_pressure(p, R);
+    Q3<T> f;
+    f.x = ad(L.y, R.y);
+    f.y = ad(ad(ad(ml(L.y, uL), ml(R.y, uR)), pL), pR);
+    f.z = ad(ad(ad(ml(L.z, uL), ml(R.z, uR)), ml(uL, pL)), ml(uR, pR));
+    return f;
+}
+// eulerSpectral, :266-292
+template <typename T>
+__device__ __forceinline__ Q3<T> eu_spectral(const Params<T> &p, Q3<T> L, Q3<T> R) {
+    T rl = sq(L.x), rr = sq(R.x);
+    Q3<T> h;
+    h.x = ml(rl, rr);
+    T hd = dv(T(1), ml(h.x, ad(rl, rr)));
+    h.y = ml(ad(ml(rl, R.y), ml(rr, L.y)), hd);
+    h.z = ml(ad(ml(rl, R.z), ml(rr, L.z)), hd);
+    T pH = eu_pressure_half(p, h);
+    return qscale(ad(sq(ml(pH, p.gam)), ab(h.y)), qsub(L, R));
+}
+// The flux sum shared by eulerStutterStep / eulerFinalStep (:308-341, :354-380),
+// on five cells s[0..4] around s[2].
+template <typename T>
+__device__ __forceinline__ Q3<T> eu_flux_sum(const Params<T> &p, const Q3<T> (&s)[5], bool fl, bool fr) {
+    const T Z = T(0);
+    // Written as in the reference: P1-P0 = 2*s1.x*s0.x*(s1.z - s0.z) + (s0.y*s0.y*s1.x - s1.y*s1.y*s0.x)
+    T pLL = fl ? Z : ad(ml(ml(ml(T(2), s[1].x), s[0].x), sb(s[1].z, s[0].z)),
+                        sb(ml(ml(s[0].y, s[0].y), s[1].x), ml(ml(s[1].y, s[1].y), s[0].x)));
+    T pL = ad(ml(ml(ml(T(2), s[2].x), s[1].x), sb(s[2].z, s[1].z)),
+              sb(ml(ml(s[1].y, s[1].y), s[2].x), ml(ml(s[2].y, s[2].y), s[1].x)));
+    T pR = ad(ml(ml(ml(T(2), s[2].x), s[3].x), sb(s[3].z, s[2].z)),
+              sb(ml(ml(s[2].y, s[2].y), s[3].x), ml(ml(s[3].y, s[3].y), s[2].x)));
+    T pRR = fr ? Z : ad(ml(ml(ml(T(2), s[3].x), s[4].x), sb(s[4].z, s[3].z)),
+                        sb(ml(ml(s[3].y, s[3].y), s[4].x), ml(ml(s[4].y, s[4].y), s[3].x)));
+
+    const bool skipL = (pLL == Z) || (pL == Z) || ((pLL < Z) != (pL < Z));
+    const bool skipM = (pL == Z) || (pR == Z) || ((pL < Z) != (pR < Z));
+    const bool skipR = (pRR == Z) || (pR == Z) || ((pRR < Z) != (pR < Z));
+
+    Q3<T> tL = skipL ? s[1] : eu_limit(s[1], s[2], dv(ml(s[0].x, pL), ml(s[2].x, pLL)));
+    Q3<T> tR = skipM ? s[2] : eu_limit(s[2], s[1], dv(ml(s[3].x, pL), ml(s[1].x, pR)));
+    Q3<T> flux = eu_flux(p, tL, tR);
+    flux = qadd(flux, eu_spectral(p, tL, tR));
+
+    tL = skipM ? s[2] : eu_limit(s[2], s[3], dv(ml(s[1].x, pR), ml(s[3].x, pL)));
+    tR = skipR ? s[3] : eu_limit(s[3], s[2], dv(ml(s[4].x, pR), ml(s[2].x, pRR)));
+    flux = qsub(flux, eu_flux(p, tL, tR));
+    flux = qsub(flux, eu_spectral(p, tL, tR));
+    return flux;
+}
+// eulerStutterStep result, :345: s2 + (0.25*dt_dx)*flux
+template <typename T>
+__device__ __forceinline__ Q3<T> eu_predict(const Params<T> &p, const Q3<T> (&s)[5], bool fl, bool fr) {
+    Q3<T> f = eu_flux_sum(p, s, fl, fr);
+    return qadd(s[2], qscale(ml(T(0.25), p.dtdx), f));
+}
+// eulerFinalStep result added to the cell, :384 and classicEuler :420
+template <typename T>
+__device__ __forceinline__ Q3<T> eu_correct(const Params<T> &p, Q3<T> u, const Q3<T> (&s)[5], bool fl, bool fr) {
+    Q3<T> f = eu_flux_sum(p, s, fl, fr);
+    return qadd(u, qscale(ml(T(0.5), p.dtdx), f));
+}
+
+}  // namespace sw

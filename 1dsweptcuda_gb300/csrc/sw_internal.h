@@ -1,0 +1,67 @@
+// Internal interface between the C ABI (api.cu) and the per-problem kernel
+// translation units (k_heat.cu, k_ks.cu, k_euler.cu).  Not installed.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/swept1d.h"
+
+namespace sw {
+
+// Kernel parameters: every constant of every scheme, in the run's precision.
+// Passed by value (constant bank), so a launch never reads a __constant__
+// symbol that another context might be rewriting.
+template <typename T>
+struct Params {
+    T fo, fo2;                 // Heat: fourier, 1 - 2 fourier
+    T c4, d2, d4, dt, dth;     // KS: 1/(4dx), 1/dx^2, 1/dx^4, dt, dt/2
+    T gam, mgam, dtdx;         // Euler
+    T bd[6];                   // Euler boundary states (rho, rho u, E) left, right
+    int64_t nx;
+    int bc;                    // SW_BC_MIRROR / PERIODIC / DIRICHLET
+};
+
+// Swept launch modes.
+enum SweptMode { MODE_UP = 0, MODE_DIAMOND = 1, MODE_DOWN = 2 };
+
+// Per (problem, precision) kernel table.  `params` points at a Params<T>
+// of the table's precision.
+struct Ops {
+    int problem;
+    int prec;        // 4 or 8
+    int R;           // stencil radius per sub-step
+    int S;           // sub-steps per time step
+    int C;           // state components per cell on the host (1 or 3)
+    size_t cell;     // bytes per cell in device layout
+    // one classic sub-step (sub 0: predictor / heat step, 1: corrector)
+    cudaError_t (*classic)(const void *params, const void *in, void *out, int sub, int64_t nx, int block,
+                           cudaStream_t s);
+    // one swept launch over all tiles of width W at `phase` (0 aligned, 1 shifted by W/2)
+    cudaError_t (*swept)(const void *params, int mode, int phase, void *state, void *slots, int64_t nx, int W,
+                         cudaStream_t s);
+    // persistent swept variant: up-triangle, n_diamonds diamonds and the down-triangle in
+    // one cooperative launch with per-half-tile phase flags; *status set non-zero on timeout.
+    cudaError_t (*persistent)(const void *params, void *state, void *slots, unsigned *flags, int *status,
+                              int64_t nx, int W, int64_t n_diamonds, cudaStream_t s);
+    // Euler host layout (3 per cell) <-> device layout (4 per cell); null for Heat/KS
+    cudaError_t (*pack)(const void *in3, void *out4, int64_t nx, cudaStream_t s);
+    cudaError_t (*unpack)(const void *in4, void *out3, int64_t nx, cudaStream_t s);
+    // dynamic shared memory a swept block of width W needs
+    size_t (*swept_smem)(int W);
+};
+
+const Ops *heat_ops(int prec);
+const Ops *ks_ops(int prec);
+const Ops *euler_ops(int prec);
+
+inline const Ops *ops_for(int problem, int prec) {
+    switch (problem) {
+    case SW_HEAT: return heat_ops(prec);
+    case SW_KS: return ks_ops(prec);
+    case SW_EULER: return euler_ops(prec);
+    default: return nullptr;
+    }
+}
+
+}  // namespace sw

@@ -1,0 +1,243 @@
+"""ctypes binding of libswept1d (include/swept1d.h).
+
+Mirrors the reference's run interface: a run is configured by the same values
+its programs take on the command line (nx, tpb, dt, tf, freq, alg) and returns
+the final state plus the snapshots the reference writes to its .dat file.
+There is no fallback: every call goes to the CUDA library, and a missing
+library is an error.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+from typing import Callable
+
+import numpy as np
+
+HEAT, KS, EULER = 0, 1, 2
+ALG_CLASSIC, ALG_SWEPT, ALG_VARIANT, ALG_SELFTEST = 0, 1, 2, 3
+BC_DEFAULT, BC_MIRROR, BC_PERIODIC, BC_DIRICHLET = 0, 1, 2, 3
+TIME_REFERENCE, TIME_STEPS = 0, 1
+COMPONENTS = {HEAT: 1, KS: 1, EULER: 3}
+PROBLEM_NAMES = {HEAT: "Heat", KS: "KS", EULER: "Euler"}
+
+ERRORS = {0: "SW_OK", -1: "SW_ERR_ARG", -2: "SW_ERR_SIZE", -3: "SW_ERR_UNSTABLE", -4: "SW_ERR_CUDA",
+          -5: "SW_ERR_NOMEM", -6: "SW_ERR_IO", -7: "SW_ERR_TIMEOUT", -8: "SW_ERR_UNSUPPORTED",
+          -9: "SW_ERR_CALLBACK", -10: "SW_ERR_USAGE"}
+
+EXPORTED = ["sw_abi_version", "sw_strerror", "sw_ctx_create", "sw_ctx_destroy", "sw_ctx_last_error",
+            "sw_config_init", "sw_validate", "sw_constants_of", "sw_initial_condition", "sw_run",
+            "sw_run_device", "sw_plan", "sw_cli_main"]
+
+
+class Config(C.Structure):
+    _fields_ = [
+        ("problem", C.c_int32), ("precision", C.c_int32), ("alg", C.c_int32), ("bc", C.c_int32),
+        ("nx", C.c_int64), ("tpb", C.c_int32), ("time_mode", C.c_int32),
+        ("dt", C.c_double), ("tf", C.c_double), ("freq", C.c_double), ("n_steps", C.c_int64),
+        ("dx", C.c_double), ("alpha", C.c_double), ("gamma", C.c_double),
+        ("left", C.c_double * 3), ("right", C.c_double * 3),
+    ]
+
+
+class Constants(C.Structure):
+    _fields_ = [
+        ("fourier", C.c_double), ("fourier_two", C.c_double),
+        ("dx_times4", C.c_double), ("dx2", C.c_double), ("dx4", C.c_double), ("dt", C.c_double),
+        ("dt_half", C.c_double), ("gam", C.c_double), ("mgam", C.c_double), ("dt_dx", C.c_double),
+        ("bd", C.c_double * 6), ("lx", C.c_double), ("dx", C.c_double),
+    ]
+
+
+class Result(C.Structure):
+    _fields_ = [
+        ("t_final", C.c_double), ("n_steps", C.c_int64), ("elapsed_ms", C.c_double),
+        ("us_per_step", C.c_double), ("kernel_ms", C.c_double), ("launches", C.c_int64),
+        ("snapshots", C.c_int32), ("tile", C.c_int32),
+    ]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class PlanInfo(C.Structure):
+    _fields_ = [("t_final", C.c_double), ("n_steps", C.c_int64), ("n_snapshots", C.c_int32),
+                ("tile", C.c_int32), ("launches", C.c_int64)]
+
+
+SNAPSHOT_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_double, C.c_void_p, C.c_int64)
+
+
+class NativeError(RuntimeError):
+    def __init__(self, code: int, message: str = ""):
+        self.code = code
+        super().__init__("%s (%d)%s" % (ERRORS.get(code, "unknown"), code, (": " + message) if message else ""))
+
+
+def library_path() -> Path:
+    return Path(__file__).resolve().parent / "lib" / "libswept1d.so"
+
+
+_lib = None
+
+
+def library():
+    """Load libswept1d.so (built by build.py / __graft_entry__.build()); raise if absent."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = library_path()
+    if not path.exists():
+        raise ImportError("libswept1d.so not built (%s); run python 1dsweptcuda_gb300/build.py" % path)
+    L = C.CDLL(str(path))
+    cp, rp, kp = C.POINTER(Config), C.POINTER(Result), C.POINTER(Constants)
+    L.sw_abi_version.restype = C.c_int
+    L.sw_strerror.argtypes = [C.c_int]
+    L.sw_strerror.restype = C.c_char_p
+    L.sw_ctx_create.argtypes = [C.c_int, C.POINTER(C.c_void_p)]
+    L.sw_ctx_destroy.argtypes = [C.c_void_p]
+    L.sw_ctx_last_error.argtypes = [C.c_void_p]
+    L.sw_ctx_last_error.restype = C.c_char_p
+    L.sw_config_init.argtypes = [cp, C.c_int, C.c_int]
+    L.sw_validate.argtypes = [cp]
+    L.sw_constants_of.argtypes = [cp, kp]
+    L.sw_initial_condition.argtypes = [cp, C.c_void_p]
+    L.sw_run.argtypes = [C.c_void_p, cp, C.c_void_p, C.c_void_p, SNAPSHOT_FN, C.c_void_p, rp]
+    L.sw_run_device.argtypes = [C.c_void_p, cp, C.c_void_p, C.c_void_p, rp]
+    L.sw_cli_main.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_char_p)]
+    L.sw_plan.argtypes = [cp, C.POINTER(PlanInfo), C.POINTER(C.c_double), C.POINTER(C.c_int64), C.c_int32]
+    for name in ("sw_ctx_create", "sw_ctx_destroy", "sw_config_init", "sw_validate", "sw_constants_of",
+                 "sw_initial_condition", "sw_run", "sw_run_device", "sw_cli_main", "sw_plan"):
+        getattr(L, name).restype = C.c_int
+    _lib = L
+    return L
+
+
+def make_config(problem: int, precision: int = 8, **kw) -> Config:
+    """A Config with the reference's defaults, then the given fields."""
+    c = Config()
+    rc = library().sw_config_init(C.byref(c), problem, precision)
+    if rc:
+        raise NativeError(rc)
+    for k, v in kw.items():
+        if k in ("left", "right"):
+            for i in range(3):
+                getattr(c, k)[i] = v[i]
+        elif not hasattr(c, k):
+            raise AttributeError("Config has no field %r" % k)
+        else:
+            setattr(c, k, v)
+    return c
+
+
+def validate(cfg: Config) -> int:
+    return library().sw_validate(C.byref(cfg))
+
+
+def constants(cfg: Config) -> Constants:
+    k = Constants()
+    rc = library().sw_constants_of(C.byref(cfg), C.byref(k))
+    if rc:
+        raise NativeError(rc)
+    return k
+
+
+def _dtype(cfg: Config):
+    return np.float64 if cfg.precision == 8 else np.float32
+
+
+def initial_condition(cfg: Config) -> np.ndarray:
+    out = np.zeros(cfg.nx * COMPONENTS[cfg.problem], dtype=_dtype(cfg))
+    rc = library().sw_initial_condition(C.byref(cfg), out.ctypes.data)
+    if rc:
+        raise NativeError(rc)
+    return out
+
+
+class Solver:
+    """One device context (stream + reusable work buffers)."""
+
+    def __init__(self, device: int = 0):
+        self._lib = library()
+        self._ctx = C.c_void_p()
+        rc = self._lib.sw_ctx_create(device, C.byref(self._ctx))
+        if rc:
+            raise NativeError(rc, "sw_ctx_create")
+
+    def close(self) -> None:
+        if self._ctx:
+            self._lib.sw_ctx_destroy(self._ctx)
+            self._ctx = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _err(self, rc: int, what: str) -> NativeError:
+        msg = self._lib.sw_ctx_last_error(self._ctx)
+        return NativeError(rc, "%s: %s" % (what, msg.decode() if msg else ""))
+
+    def run(self, cfg: Config, ic: np.ndarray | None = None,
+            on_snapshot: Callable[[float, np.ndarray], None] | None = None):
+        """Host-to-host run (sw_run).  Returns (final_state, Result, snapshots),
+        snapshots = [(t, state)] at the reference's output times."""
+        dtype = _dtype(cfg)
+        n = cfg.nx * COMPONENTS[cfg.problem]
+        if ic is None:
+            ic = initial_condition(cfg)
+        ic = np.ascontiguousarray(ic, dtype=dtype)
+        if ic.size != n:
+            raise ValueError("initial condition has %d values, expected %d" % (ic.size, n))
+        final = np.empty(n, dtype=dtype)
+        snaps: list[tuple[float, np.ndarray]] = []
+
+        def cb(_user, t, ptr, nx):
+            arr = np.ctypeslib.as_array(C.cast(ptr, C.POINTER(C.c_double if dtype == np.float64 else C.c_float)),
+                                        shape=(n,)).copy()
+            snaps.append((t, arr))
+            if on_snapshot is not None:
+                on_snapshot(t, arr)
+            return 0
+
+        cbf = SNAPSHOT_FN(cb)
+        res = Result()
+        rc = self._lib.sw_run(self._ctx, C.byref(cfg), ic.ctypes.data, final.ctypes.data, cbf, None, C.byref(res))
+        if rc:
+            raise self._err(rc, "sw_run")
+        return final, res, snaps
+
+    def run_device(self, cfg: Config, state_ptr: int, stream: int = 0) -> Result:
+        """Device-resident run (sw_run_device) on a device pointer in device layout
+        (Euler: 4 values per cell).  Blocks until the run completes."""
+        res = Result()
+        rc = self._lib.sw_run_device(self._ctx, C.byref(cfg), C.c_void_p(state_ptr),
+                                     C.c_void_p(stream) if stream else None, C.byref(res))
+        if rc:
+            raise self._err(rc, "sw_run_device")
+        return res
+
+
+def plan(cfg: Config, cap: int = 4096):
+    """sw_plan: (PlanInfo, snapshot times, step count at each snapshot) -- no device needed."""
+    info = PlanInfo()
+    t = (C.c_double * cap)()
+    s = (C.c_int64 * cap)()
+    rc = library().sw_plan(C.byref(cfg), C.byref(info), t, s, cap)
+    if rc:
+        raise NativeError(rc, "sw_plan")
+    n = min(info.n_snapshots, cap)
+    return info, list(t[:n]), list(s[:n])
+
+
+def cli_main(problem: int, precision: int, argv: list[str]) -> int:
+    """sw_cli_main with argv (argv[0] = program name) -- the bin/*Out programs in-process."""
+    arr = (C.c_char_p * (len(argv) + 1))(*[a.encode() for a in argv], None)
+    return library().sw_cli_main(problem, precision, len(argv), arr)

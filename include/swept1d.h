@@ -1,0 +1,186 @@
+/*
+ * swept1d -- GB300 (sm_103a) swept-rule and classic solvers for the 1D heat
+ * (FTCS), Kuramoto-Sivashinsky and Euler/Sod problems.  C ABI.
+ *
+ * The reference (Niemeyer-Research-Group/1DSweptCUDA) has no library: its
+ * public surface is three programs, SweptSource/{Heat,KS,Euler}1D_SweptShared.cu,
+ * built as bin/<Problem><Single|Double>Out and driven by argv
+ * (`nx tpb dt tf freq alg solution.dat [timing.txt]`).  Each entry point below
+ * replaces one piece of those programs; the citation is on each declaration.
+ * bin/<Problem><Precision>Out of this project is a thin main() over
+ * sw_cli_main().
+ *
+ * Conventions
+ *  - Every function returns SW_OK (0) or a negative SW_ERR_* code; nothing
+ *    throws across the ABI.  sw_strerror() names a code, sw_ctx_last_error()
+ *    gives the message of the last failure on a context.
+ *  - Host state layout (ic_host / final_host / snapshots): REAL[nx] for Heat
+ *    and KS; REAL[3*nx] of (rho, rho*u, E) per cell for Euler -- the layout of
+ *    the reference's REAL / REALthree host arrays.  REAL is float when
+ *    precision == 4, double when precision == 8.
+ *  - Device state layout (sw_run_device): REAL[nx] for Heat/KS; for Euler
+ *    REAL[4*nx] of (rho, rho*u, E, pad) per cell (a double4/float4 array).
+ *  - A context owns one CUDA stream and the device work buffers; it is
+ *    reusable across runs and is not thread-safe (one host thread at a time).
+ */
+#ifndef SWEPT1D_H
+#define SWEPT1D_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SW_ABI_VERSION 1
+
+/* ---------------------------------------------------------------- codes */
+enum sw_status {
+    SW_OK = 0,
+    SW_ERR_ARG = -1,         /* null pointer or unknown enum value */
+    SW_ERR_SIZE = -2,        /* nx / tpb rule broken (Heat1D_SweptShared.cu:735-740) */
+    SW_ERR_UNSTABLE = -3,    /* Euler dt/dx > 0.21 (Euler1D_SweptShared.cu:1168-1172) */
+    SW_ERR_CUDA = -4,        /* a CUDA call or kernel failed */
+    SW_ERR_NOMEM = -5,       /* device or pinned host allocation failed */
+    SW_ERR_IO = -6,          /* output file could not be opened or written */
+    SW_ERR_TIMEOUT = -7,     /* a bounded inter-block wait expired; state not valid */
+    SW_ERR_UNSUPPORTED = -8, /* valid request this build does not provide */
+    SW_ERR_CALLBACK = -9,    /* the snapshot callback asked to stop */
+    SW_ERR_USAGE = -10       /* too few command-line arguments (argc < 8) */
+};
+
+enum sw_problem { SW_HEAT = 0, SW_KS = 1, SW_EULER = 2 };
+
+/* alg: the reference's 6th argument (Heat1D_SweptShared.cu:717) */
+enum sw_alg {
+    SW_ALG_CLASSIC = 0,  /* one launch per (sub-)step, ping-pong arrays */
+    SW_ALG_SWEPT = 1,    /* shared-memory swept rule: up-triangle, diamonds, down-triangle */
+    SW_ALG_VARIANT = 2,  /* GPU-only variant: persistent swept kernel (Heat, Euler);
+                            KS: 32-point warp nodes, the reference's register path cycle */
+    SW_ALG_SELFTEST = 3  /* KS only: warp-node kernels vs shared kernels (KS1D_SweptShared.cu:681-751) */
+};
+
+enum sw_bc {
+    SW_BC_DEFAULT = 0,   /* the reference's: Heat mirror, KS periodic, Euler Dirichlet */
+    SW_BC_MIRROR = 1,    /* insulated ends (Heat) */
+    SW_BC_PERIODIC = 2,  /* periodic (Heat, KS) */
+    SW_BC_DIRICHLET = 3  /* cells 0 and nx-1 held at the boundary states (Euler) */
+};
+
+enum sw_time_mode {
+    SW_TIME_REFERENCE = 0, /* the reference wrappers' t_eq bookkeeping from dt, tf, freq */
+    SW_TIME_STEPS = 1      /* exactly n_steps time steps (swept finishes the remainder classically) */
+};
+
+/* ------------------------------------------------------------ run config */
+typedef struct sw_config {
+    int32_t problem;     /* enum sw_problem */
+    int32_t precision;   /* 4 = float (Single), 8 = double (Double) */
+    int32_t alg;         /* enum sw_alg */
+    int32_t bc;          /* enum sw_bc */
+    int64_t nx;          /* spatial points (argv[1]) */
+    int32_t tpb;         /* points per swept node = threads per block (argv[2]) */
+    int32_t time_mode;   /* enum sw_time_mode */
+    double dt;           /* time step (argv[3]) */
+    double tf;           /* finish time as given (argv[4]); the library applies tf - dt/4 like main() */
+    double freq;         /* output interval (argv[5]); <= 0 or >= tf: no intermediate snapshots */
+    int64_t n_steps;     /* SW_TIME_STEPS only */
+    /* physics; 0 selects the reference's constant */
+    double dx;           /* Heat 0.001, KS 0.5, Euler 1/(nx-2) */
+    double alpha;        /* Heat diffusivity 8.418e-5 */
+    double gamma;        /* Euler heat-capacity ratio 1.4 */
+    double left[3];      /* Euler left state (rho, u, p); all 0 = Sod (1, 0, 1) */
+    double right[3];     /* Euler right state (rho, u, p); all 0 = Sod (0.125, 0, 0.1) */
+} sw_config;
+
+/* Derived constants, rounded to the run's precision exactly as the
+ * reference's main() rounds them (Heat1D_SweptShared.cu:719-728,
+ * KS1D_SweptShared.cu:917-926, Euler1D_SweptShared.cu:1127-1154). */
+typedef struct sw_constants {
+    double fourier, fourier_two;                  /* Heat */
+    double dx_times4, dx2, dx4, dt, dt_half;      /* KS (reciprocals) */
+    double gam, mgam, dt_dx;                      /* Euler */
+    double bd[6];                                 /* Euler boundary states (rho, rho u, E) x 2 */
+    double lx, dx;                                /* domain length and spacing as the .dat header prints them */
+} sw_constants;
+
+typedef struct sw_result {
+    double t_final;     /* simulated time reached, as the reference wrappers return it (t_eq) */
+    int64_t n_steps;    /* time steps actually advanced */
+    double elapsed_ms;  /* event time around the whole run: allocation, copies, stepping, snapshots */
+    double us_per_step; /* elapsed_ms*1e3 / (t_final/dt): the reference's timing-file figure */
+    double kernel_ms;   /* device time of the stepping launches alone */
+    int64_t launches;   /* kernel launches issued */
+    int32_t snapshots;  /* intermediate snapshots delivered */
+    int32_t tile;       /* tile width used by the swept / variant path */
+} sw_result;
+
+/* Intermediate output, called with the host state at each output time
+ * (replaces the in-wrapper .dat row writes, Heat1D_SweptShared.cu:497-509,
+ * 660-678).  Return 0 to continue, non-zero to stop the run. */
+typedef int (*sw_snapshot_fn)(void *user, double t, const void *state_host, int64_t nx);
+
+typedef struct sw_ctx sw_ctx;
+
+/* ---------------------------------------------------------- entry points */
+int sw_abi_version(void);
+const char *sw_strerror(int code);
+
+/* Create / destroy a context on a CUDA device (replaces cudaSetDevice(GPUNUM)
+ * and the per-run cudaMalloc/cudaFree pairs, Heat1D_SweptShared.cu:709,
+ * 530-536, 688-692). */
+int sw_ctx_create(int device, sw_ctx **out);
+int sw_ctx_destroy(sw_ctx *ctx);
+const char *sw_ctx_last_error(const sw_ctx *ctx);
+
+/* Fill a config with the reference's defaults for a problem/precision. */
+int sw_config_init(sw_config *cfg, int problem, int precision);
+
+/* main()'s input checks (Heat1D_SweptShared.cu:735-740, KS1D_SweptShared.cu:897-902,
+ * Euler1D_SweptShared.cu:1161-1172). */
+int sw_validate(const sw_config *cfg);
+
+/* The derived constants (main(), see sw_constants). */
+int sw_constants_of(const sw_config *cfg, sw_constants *out);
+
+/* The reference's initial condition, initFun (Heat1D_SweptShared.cu:60-66,751-754;
+ * KS1D_SweptShared.cu:67-72,945; Euler1D_SweptShared.cu:1179). */
+int sw_initial_condition(const sw_config *cfg, void *ic_host);
+
+/* One run from a host initial condition to a host final state: replaces
+ * classicWrapper / sweptWrapper (Heat1D_SweptShared.cu:470-695,
+ * KS1D_SweptShared.cu:595-864, Euler1D_SweptShared.cu:837-1110).
+ * cb may be NULL. */
+int sw_run(sw_ctx *ctx, const sw_config *cfg, const void *ic_host, void *final_host,
+           sw_snapshot_fn cb, void *user, sw_result *out);
+
+/* The same run on a device-resident state (updated in place, device layout),
+ * enqueued on `stream` (a cudaStream_t; NULL = the context's stream).  No
+ * snapshots; returns when the run has completed. */
+int sw_run_device(sw_ctx *ctx, const sw_config *cfg, void *state_dev, void *stream, sw_result *out);
+
+/* What a run would do, without a device: the time bookkeeping of
+ * classicWrapper / sweptWrapper (Heat1D_SweptShared.cu:483-510,541-682;
+ * KS1D_SweptShared.cu:609-631,676-851; Euler1D_SweptShared.cu:855-888,924-1100).
+ * Fills the final t_eq, the time steps advanced and the snapshot count; if
+ * snap_t / snap_steps are non-NULL, up to `cap` snapshot times and the step
+ * count at each are written. */
+typedef struct sw_plan_info {
+    double t_final;
+    int64_t n_steps;
+    int32_t n_snapshots;
+    int32_t tile;        /* swept / variant tile width (0 for classic) */
+    int64_t launches;    /* kernel launches the run will issue (launch-per-pass paths) */
+} sw_plan_info;
+int sw_plan(const sw_config *cfg, sw_plan_info *out, double *snap_t, int64_t *snap_steps, int32_t cap);
+
+/* The whole program: argv exactly as bin/<Problem><Precision>Out takes it
+ * (replaces main(), Heat1D_SweptShared.cu:697-836, KS1D_SweptShared.cu:866-1029,
+ * Euler1D_SweptShared.cu:1112-1287).  Writes solution.dat and appends the
+ * timing row like the reference.  Returns 0 or a negative code. */
+int sw_cli_main(int problem, int precision, int argc, char **argv);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SWEPT1D_H */

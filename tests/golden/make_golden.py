@@ -1,0 +1,112 @@
+"""Generate the golden fixtures in this folder from the reference itself.
+
+Run in a checkout where the reference sources exist (default
+/root/reference/SweptSource, override with SWEPT1D_REFERENCE_SRC):
+
+    python tests/golden/make_golden.py
+
+It writes
+
+* ``ref_classic.npz`` -- for Heat, KS and Euler in float and double: the
+  reference's own initial condition (its ``initFun``) and the state after N
+  classic steps computed by the reference's own stencil functions
+  (``execFunc``; ``stutterStep``/``finalStep``; ``eulerStutterStep``/
+  ``eulerFinalStep``) compiled host-side from the unmodified reference files
+  by ``oracle/ref_harness.cu``; for Euler also the reference's ``pressure`` and
+  ``energy`` of that state (the .dat writer's derived rows).
+* ``ks_official.npz`` -- the reference's KS golden run,
+  ``SweptSource/Testing/KSDouble_Official.txt`` (nx=1024, dx=0.5, FP64 swept,
+  dt=1e-7; Velocity at t = 0, 6, 12, 18, 20), parsed to arrays.
+
+The tests read only these .npz files; they never touch the reference.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parent.parent
+sys.path.insert(0, str(ROOT))
+
+from oracle import build as obuild  # noqa: E402
+import oracle as O  # noqa: E402
+
+# (problem, nx, dt, nsteps): chosen so every scheme moves visibly.
+CASES = [
+    (O.HEAT, 256, 0.004, 500),      # Fo = 0.337, insulated ends
+    (O.KS, 256, 0.005, 400),        # periodic, t = 2
+    (O.EULER, 256, 0.1 / 254, 400),  # dt/dx = 0.1, t = 0.157 (shock well formed)
+]
+NAMES = {O.HEAT: "heat", O.KS: "ks", O.EULER: "euler"}
+
+
+def _run_reference(problem, prec, nx, dt, nsteps):
+    L = C.CDLL(str(obuild.ref_lib_path(problem, prec)))
+    dtype = np.float64 if prec == 8 else np.float32
+    assert L.ref_real_size() == prec
+    c = O.reference_consts(problem, prec, nx, dt)
+    vp = C.c_void_p
+    if problem == O.EULER:
+        ic = O.reference_ic(problem, prec, nx)  # the reference builds it from bd[] (Euler1D...cu:1179)
+        b6 = (C.c_double * 6)(*c.bd)
+        L.ref_set(C.c_int64(nx), C.c_double(c.gam), C.c_double(c.mgam), C.c_double(c.dt_dx), b6)
+        fin = ic.copy()
+        L.ref_classic(vp(fin.ctypes.data), C.c_int64(nx), C.c_int64(nsteps))
+        p = np.zeros(nx, dtype)
+        e = np.zeros(nx, dtype)
+        L.ref_derived(vp(fin.ctypes.data), C.c_int64(nx), vp(p.ctypes.data), vp(e.ctypes.data))
+        return ic, fin, {"pressure": p, "energy": e}
+    ic = np.zeros(nx, dtype)
+    L.ref_ic(C.c_int64(nx), vp(ic.ctypes.data))
+    fin = ic.copy()
+    if problem == O.HEAT:
+        L.ref_classic(vp(fin.ctypes.data), C.c_int64(nx), C.c_double(c.fourier), C.c_double(c.fourier_two),
+                      C.c_int64(nsteps))
+    else:
+        L.ref_classic(vp(fin.ctypes.data), C.c_int64(nx), C.c_double(c.dx_times4), C.c_double(c.dx2),
+                      C.c_double(c.dx4), C.c_double(c.dt), C.c_double(c.dt_half), C.c_int64(nsteps))
+    return ic, fin, {}
+
+
+def make_ref_classic():
+    libs = obuild.build_ref()
+    if not libs:
+        raise SystemExit("reference sources not found at %s" % obuild.REFERENCE_SRC)
+    out = {}
+    for problem, nx, dt, nsteps in CASES:
+        for prec in (8, 4):
+            key = "%s_f%d" % (NAMES[problem], 8 * prec)
+            ic, fin, extra = _run_reference(problem, prec, nx, dt, nsteps)
+            out[key + "_ic"] = ic
+            out[key + "_final"] = fin
+            out[key + "_meta"] = np.array([nx, dt, nsteps], dtype=np.float64)
+            for k, v in extra.items():
+                out[key + "_" + k] = v
+    np.savez_compressed(HERE / "ref_classic.npz", **out)
+
+
+def make_ks_official():
+    src = obuild.REFERENCE_SRC / "Testing" / "KSDouble_Official.txt"
+    lines = src.read_text().splitlines()
+    head = lines[0].split()
+    times, rows = [], []
+    for ln in lines[1:]:
+        parts = ln.split()
+        if not parts:
+            continue
+        assert parts[0] == "Velocity"
+        times.append(float(parts[1]))
+        rows.append([float(v) for v in parts[2:]])
+    np.savez_compressed(HERE / "ks_official.npz", header=np.array([float(h) for h in head]),
+                        times=np.array(times), velocity=np.array(rows))
+
+
+if __name__ == "__main__":
+    make_ref_classic()
+    make_ks_official()
+    for f in ("ref_classic.npz", "ks_official.npz"):
+        print(f, (HERE / f).stat().st_size, "bytes")
