@@ -159,6 +159,11 @@ Params<T> make_params(const sw_config &c, const sw_constants &k) {
     for (int i = 0; i < 6; ++i) p.bd[i] = (T)k.bd[i];
     p.nx = c.nx;
     p.bc = resolved_bc(c);
+    auto is_pow2 = [](T v) {
+        int e = 0;
+        return v > T(0) && std::isfinite((double)v) && std::frexp((double)v, &e) == 0.5;
+    };
+    p.pow2 = (c.problem == SW_KS && is_pow2(p.c4) && is_pow2(p.d2) && is_pow2(p.d4)) ? 1 : 0;
     return p;
 }
 

@@ -20,6 +20,7 @@ struct Params {
     T bd[6];                   // Euler boundary states (rho, rho u, E) left, right
     int64_t nx;
     int bc;                    // SW_BC_MIRROR / PERIODIC / DIRICHLET
+    int pow2;                  // KS: c4, d2, d4 are exact powers of two (products by them are exact)
 };
 
 // Swept launch modes.

@@ -1,0 +1,103 @@
+"""Performance sweep (the role of the reference's quickperform.py / runTest.sh):
+time classic, swept and variant over problems, precisions, nx and tpb with the
+state resident on the device, and check that all paths agree bit for bit.
+
+    python 1dsweptcuda_gb300/perf.py [--quick] [--json out.json]
+
+Each case runs SW_TIME_STEPS with a step count that is a whole number of swept
+cycles for every tpb in the case, timed with CUDA events inside the library
+(sw_result.kernel_ms).  Prints one row per case and the swept/classic ratio.
+"""
+from __future__ import annotations
+
+import argparse
+import importlib
+import json
+import sys
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent.parent
+sys.path.insert(0, str(ROOT))
+
+
+def cases(quick: bool):
+    # (label, problem, precision, bc, nx, [tpb...], steps, dt)
+    big = 1 << 22
+    c = [
+        ("heat-periodic nx=4096 (Fo=0.1)", 0, 8, 2, 4096, [128], 20480, 1.18793e-3),
+        ("ks nx=2^20", 1, 8, 0, 1 << 20, [256], 4096, 0.005),
+        ("heat nx=2^22", 0, 8, 0, big, [256, 1024], 4096, 0.004),
+        ("heat nx=2^22", 0, 4, 0, big, [256, 1024], 4096, 0.004),
+        ("ks nx=2^22", 1, 8, 0, big, [256, 1024], 2048, 0.005),
+        ("ks nx=2^22", 1, 4, 0, big, [256, 1024], 2048, 0.005),
+        ("euler nx=2^22", 2, 8, 0, big, [256, 512], 256, 0.1 / (big - 2)),
+        ("euler nx=2^22", 2, 4, 0, big, [256, 512], 256, 0.1 / (big - 2)),
+    ]
+    if quick:
+        c = [x for x in c if x[4] <= (1 << 20)]
+    return c
+
+
+def main():
+    import numpy as np
+    import torch
+
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--quick", action="store_true")
+    ap.add_argument("--json", default=None)
+    args = ap.parse_args()
+    sw = importlib.import_module("1dsweptcuda_gb300")
+    solver = sw.Solver(0)
+    stream = torch.cuda.current_stream()
+    rows = []
+    for label, prob, prec, bc, nx, tpbs, steps, dt in cases(args.quick):
+        dtype = torch.float64 if prec == 8 else torch.float32
+        results = {}
+        for tpb in tpbs:
+            for alg in (sw.ALG_CLASSIC, sw.ALG_SWEPT, sw.ALG_VARIANT):
+                if alg == sw.ALG_CLASSIC and tpb != tpbs[0]:
+                    continue
+                cfg = sw.make_config(prob, prec, alg=alg, nx=nx, tpb=tpb, dt=dt, bc=bc,
+                                     time_mode=sw.TIME_STEPS, n_steps=steps)
+                ic = sw.initial_condition(cfg)
+                if prob == 2:
+                    dev = np.zeros((nx, 4), dtype=ic.dtype)
+                    dev[:, :3] = ic.reshape(-1, 3)
+                    ic = dev.ravel()
+                elif prob == 0 and bc == 2:
+                    x = np.arange(nx)
+                    ic = (50 + 100 * np.sin(2 * np.pi * x / nx)).astype(ic.dtype)
+                st = torch.from_numpy(ic).cuda()
+                solver.run_device(cfg, st.data_ptr(), stream.cuda_stream)  # warm
+                st = torch.from_numpy(ic).cuda()
+                torch.cuda.synchronize()
+                res = solver.run_device(cfg, st.data_ptr(), stream.cuda_stream)
+                out = st.cpu().numpy()
+                ups = nx * steps / (res.kernel_ms * 1e-3)
+                key = ("classic" if alg == 0 else "swept" if alg == 1 else "variant", tpb)
+                results[key] = (ups, out, res)
+                row = {"case": label, "precision": prec, "alg": key[0], "tpb": tpb if alg else None,
+                       "tile": res.tile, "nx": nx, "steps": steps, "ms": res.kernel_ms,
+                       "cell_updates_per_s": ups, "launches": res.launches,
+                       "finite": bool(np.isfinite(out).all())}
+                rows.append(row)
+        base = results[("classic", tpbs[0])]
+        for (name, tpb), (ups, out, res) in results.items():
+            same = np.array_equal(out, base[1])
+            for r in rows:
+                if r["case"] == label and r["precision"] == prec and r["alg"] == name and \
+                        (r["tpb"] == tpb or name == "classic"):
+                    r["equal_to_classic"] = bool(same)
+                    r["over_classic"] = ups / base[0]
+        for r in rows:
+            if r["case"] == label and r["precision"] == prec:
+                print("%-34s f%-2d %-8s tpb=%-5s %10.3e cell-updates/s  x%.2f vs classic  %s" % (
+                    label, prec * 8, r["alg"], r["tpb"], r["cell_updates_per_s"], r.get("over_classic", 1.0),
+                    "bit-identical" if r.get("equal_to_classic") else "DIFFERS"), flush=True)
+    solver.close()
+    if args.json:
+        Path(args.json).write_text(json.dumps(rows, indent=1))
+
+
+if __name__ == "__main__":
+    main()

@@ -40,10 +40,10 @@ DT = 0.005
 TF = 200.0
 NSTEPS = 40000            # tf / dt
 B_CLASSIC_KS_F64 = 40     # algorithmic bytes per cell-update of the classic KS FP64 scheme
-DP_OPS_PER_UPDATE = 40    # FP64 operations per cell-update (2 sub-steps x 20, none fused)
-# FP64 pipe rate of the GB300 measured with a DFMA/DADD throughput probe ("FP64 pipe"),
-# in FP64 operations per second; used only for the fp64_pipe fraction.
-FP64_OPS_PEAK = None
+DP_OPS_PER_UPDATE = 30    # FP64 instructions per cell-update: 2 sub-steps x 15 (exact power-of-two folds)
+# FP64 pipe issue rate of this GB300 pool, measured with a DFMA throughput
+# probe: 0.600e12 DFMA/s (2.06 per clock per SM at 1.92 GHz; 1.2 TFLOP/s).
+FP64_OPS_PEAK = 0.600e12
 BASELINE_K40_KS_F64_SWEPT = 1.07e10  # KS FP64 swept, nx=2^20, K40c
 
 
@@ -113,6 +113,22 @@ def _dist():
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     return world, rank, local
+
+
+def replica_throughput(local_ms: float, units: float) -> tuple[float, float]:
+    """Whole-job throughput of N independent replicas: every rank processed
+    `units` cell-updates in `local_ms`; the job took the slowest rank's time.
+    Returns (N * units / max_ms in units/s, max_ms).  Single process: no collective."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()):
+        return units / (local_ms * 1e-3), local_ms
+    world = dist.get_world_size()
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([local_ms], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    max_ms = float(t.item())
+    return world * units / (max_ms * 1e-3), max_ms
 
 
 def cpu_baseline(seconds: float = 10.0, threads: int | None = None) -> dict:
@@ -209,14 +225,10 @@ def run_ours(args) -> None:
             kern_launch += res.launches
         torch.cuda.synchronize()
     clocks = clk.summary()
-    total_ms = sum(times)
+    value, total_ms = replica_throughput(sum(times), float(NX) * NSTEPS * args.steps)
     if world > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
         dist.barrier()
     ms_per_step = total_ms / args.steps
-    value = world * NX * NSTEPS / (ms_per_step * 1e-3)
 
     final = state.cpu().numpy()
     assert np.isfinite(final).all()

@@ -34,17 +34,22 @@ def heat_series(t: float, divs: int, alpha: float = 8.418e-5, dx: float = 0.001,
 
 
 def heat_periodic_mode(nsteps: int, nx: int, fourier: float, mean: float = 50.0, amp: float = 100.0,
-                       discrete: bool = True, alpha: float = 8.418e-5, dx: float = 0.001) -> np.ndarray:
+                       discrete: bool = True, alpha: float = 8.418e-5, dx: float = 0.001,
+                       fourier_two: float | None = None) -> np.ndarray:
     """Periodic heat, IC mean + amp sin(2 pi x/L), L = nx dx, after nsteps FTCS steps.
-    discrete=True: the scheme's own exact answer (factor g = 1 - 4 Fo sin^2(pi/nx) per step);
+    discrete=True: the scheme's own exact answer -- per step the mean is
+    multiplied by fo2 + 2 fo and the mode by fo2 + 2 fo cos(2 pi/nx), with
+    fo2 = 1 - 2 fo unless the run's rounded value is given;
     discrete=False: the PDE's exp(-alpha (2 pi/L)^2 t), t = nsteps * Fo dx^2/alpha."""
     x = np.arange(nx) * dx
     L = nx * dx
     if discrete:
-        g = (1.0 - 4.0 * fourier * math.sin(math.pi / nx) ** 2) ** nsteps
-    else:
-        t = nsteps * fourier * dx * dx / alpha
-        g = math.exp(-alpha * (2 * math.pi / L) ** 2 * t)
+        fo2 = (1.0 - 2.0 * fourier) if fourier_two is None else fourier_two
+        g0 = (fo2 + 2.0 * fourier) ** nsteps
+        g = (fo2 + 2.0 * fourier * math.cos(2 * math.pi / nx)) ** nsteps
+        return mean * g0 + amp * g * np.sin(2 * np.pi * x / L)
+    t = nsteps * fourier * dx * dx / alpha
+    g = math.exp(-alpha * (2 * math.pi / L) ** 2 * t)
     return mean + amp * g * np.sin(2 * np.pi * x / L)
 
 
