@@ -29,9 +29,9 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # operation with a round-to-nearest intrinsic, so they never depend on it.
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC",
                      "-Xptxas", "-warn-spills", "-I", str(INCLUDE)]
-CU_SOURCES = ["k_heat.cu", "k_ks.cu", "k_euler.cu", "api.cu"]
+CU_SOURCES = ["k_heat.cu", "k_ks.cu", "k_euler.cu", "api.cu", "batch.cu"]
 CPP_SOURCES = ["cli.cpp"]
-HEADERS = ["engine.cuh", "stencils.cuh", "persistent.cuh", "sw_internal.h"]
+HEADERS = ["engine.cuh", "stencils.cuh", "persistent.cuh", "sw_internal.h", "ctx.h"]
 PROGRAMS = [(p, pi, q, qi) for pi, p in enumerate(("Heat", "KS", "Euler")) for q, qi in (("Single", 4), ("Double", 8))]
 
 
@@ -71,8 +71,10 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         o = OBJ / (src + ".o")
         objs.append(o)
         if force or _stale(o, [CSRC / src, INCLUDE / "swept1d.h"]):
+            # -ffp-contract=off: the .dat writer's derived rows (velocity, energy, pressure)
+            # must round like the reference's unfused host code, also where g++ would fuse
             jobs.append(["g++", "-c", str(CSRC / src), "-o", str(o), "-O2", "-std=c++17", "-fPIC",
-                         "-I", str(INCLUDE)])
+                         "-ffp-contract=off", "-I", str(INCLUDE)])
     if jobs:
         with ThreadPoolExecutor(max_workers=min(8, len(jobs))) as ex:
             for cmd in jobs:

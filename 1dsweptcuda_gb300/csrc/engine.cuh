@@ -201,19 +201,17 @@ __device__ __forceinline__ void tile_up(const Params<T> &p, T *rows, int L, int 
     }
 }
 
-// One swept pass over all tiles.  MODE_UP: state -> up-triangle -> slots
-// (phase 0 only).  MODE_DIAMOND: slots -> down + up -> slots.  MODE_DOWN:
-// slots -> down-triangle -> state.  Block = one tile.
+// One swept pass of tile t of a periodic / bounded domain of p.nx cells whose
+// state and slots start at `state` and `slots`.  MODE_UP: state ->
+// up-triangle -> slots (phase 0 only).  MODE_DIAMOND: slots -> down + up ->
+// slots.  MODE_DOWN: slots -> down-triangle -> state.
 template <int P, typename T, int MODE>
-__global__ void __launch_bounds__(Scheme<P, T>::MAXT) k_swept(const Params<T> p, typename Scheme<P, T>::G *__restrict__ state,
-                                                typename Scheme<P, T>::G *__restrict__ slots, const int W,
-                                                const int phase) {
-    using G = typename Scheme<P, T>::G;
+__device__ __forceinline__ void swept_tile(const Params<T> &p, typename Scheme<P, T>::G *__restrict__ state,
+                                           typename Scheme<P, T>::G *__restrict__ slots, T *rows, const int W,
+                                           const int phase, const int64_t t) {
     constexpr int R = Scheme<P, T>::R;
-    extern __shared__ __align__(16) unsigned char sw_smem[];
-    T *rows = reinterpret_cast<T *>(sw_smem);
     const int L = W + 2 * R, h = W >> 1;
-    const int64_t nx = p.nx, nhalf = nx / h, t = blockIdx.x;
+    const int64_t nx = p.nx, nhalf = nx / h;
     const int64_t base = t * W + (int64_t)phase * h;
     const int64_t hl = (2 * t + phase) % nhalf;
     const int64_t hr = (hl + 1 == nhalf) ? 0 : hl + 1;
@@ -237,14 +235,23 @@ __global__ void __launch_bounds__(Scheme<P, T>::MAXT) k_swept(const Params<T> p,
     }
 }
 
-// One classic sub-step over all cells: classicHeat (Heat1D_SweptShared.cu:132-145),
-// classicKS (KS1D_SweptShared.cu:189-207), classicEuler (Euler1D_SweptShared.cu:400-426).
+// One swept pass over all tiles of one domain; block = one tile.
+template <int P, typename T, int MODE>
+__global__ void __launch_bounds__(Scheme<P, T>::MAXT) k_swept(const Params<T> p, typename Scheme<P, T>::G *__restrict__ state,
+                                                typename Scheme<P, T>::G *__restrict__ slots, const int W,
+                                                const int phase) {
+    extern __shared__ __align__(16) unsigned char sw_smem[];
+    swept_tile<P, T, MODE>(p, state, slots, reinterpret_cast<T *>(sw_smem), W, phase, (int64_t)blockIdx.x);
+}
+
+// One classic sub-step at cell g of a domain of p.nx cells: classicHeat
+// (Heat1D_SweptShared.cu:132-145), classicKS (KS1D_SweptShared.cu:189-207),
+// classicEuler (Euler1D_SweptShared.cu:400-426).
 template <int P, typename T>
-__global__ void __launch_bounds__(Scheme<P, T>::MAXT) k_classic(const Params<T> p, const typename Scheme<P, T>::G *__restrict__ in,
-                                                  typename Scheme<P, T>::G *__restrict__ out, const int sub) {
-    const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void classic_cell(const Params<T> &p, const typename Scheme<P, T>::G *__restrict__ in,
+                                             typename Scheme<P, T>::G *__restrict__ out, const int sub,
+                                             const int64_t g) {
     const int64_t nx = p.nx;
-    if (g >= nx) return;
     if constexpr (P == SW_HEAT) {
         int64_t l = g - 1, r = g + 1;
         if (p.bc == SW_BC_PERIODIC) {
@@ -287,6 +294,13 @@ __global__ void __launch_bounds__(Scheme<P, T>::MAXT) k_classic(const Params<T> 
         }
         out[g] = V4<T>{o.x, o.y, o.z, T(0)};
     }
+}
+
+template <int P, typename T>
+__global__ void __launch_bounds__(Scheme<P, T>::MAXT) k_classic(const Params<T> p, const typename Scheme<P, T>::G *__restrict__ in,
+                                                  typename Scheme<P, T>::G *__restrict__ out, const int sub) {
+    const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g < p.nx) classic_cell<P, T>(p, in, out, sub, g);
 }
 
 // Euler host layout (rho, rho u, E) <-> device layout (rho, rho u, E, 0).

@@ -20,6 +20,9 @@ Ops make_ops() {
     o.pack = launch_pack<T>;
     o.unpack = launch_unpack<T>;
     o.swept_smem = smem_of<SW_EULER, T>;
+    o.batch_swept = launch_swept_batch<SW_EULER, T>;
+    o.batch_classic = launch_classic_batch<SW_EULER, T>;
+    o.batch_persistent = launch_persistent_batch<SW_EULER, T>;
     return o;
 }
 }  // namespace

@@ -20,6 +20,9 @@ Ops make_ops() {
     o.pack = nullptr;
     o.unpack = nullptr;
     o.swept_smem = smem_of<SW_KS, T>;
+    o.batch_swept = launch_swept_batch<SW_KS, T>;
+    o.batch_classic = launch_classic_batch<SW_KS, T>;
+    o.batch_persistent = launch_persistent_batch<SW_KS, T>;
     return o;
 }
 }  // namespace

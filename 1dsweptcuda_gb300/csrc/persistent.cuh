@@ -94,50 +94,113 @@ __device__ __forceinline__ void tile_import_cg(T *rows, int L, int W, const type
     }
 }
 
+// Stage q of tile t of one domain (state / slots / flags at the domain's
+// base).  Returns false if a wait gave up.
+template <int P, typename T>
+__device__ __forceinline__ bool persistent_tile(const Params<T> &p, typename Scheme<P, T>::G *__restrict__ state,
+                                                typename Scheme<P, T>::G *__restrict__ slots, unsigned *flags,
+                                                int *status, T *rows, const int W, const int64_t q,
+                                                const int64_t last, const int64_t t) {
+    const int L = W + 2 * Scheme<P, T>::R, h = W >> 1;
+    const int64_t nx = p.nx, nhalf = nx / h;
+    const int phase = (int)(q & 1);
+    const int64_t base = t * W + (int64_t)phase * h;
+    const int64_t hl = (2 * t + phase) % nhalf;
+    const int64_t hr = (hl + 1 == nhalf) ? 0 : hl + 1;
+    if (q == 0) {
+        for (int x = threadIdx.x; x < W; x += blockDim.x) tile_put<P, T>(rows, L, 0, x, state[base + x]);
+    } else {
+        if (!wait_slots(flags, hl, hr, (unsigned)q, status)) return false;
+        tile_import_cg<P, T>(rows, L, W, slots + hl * W, slots + hr * W);
+    }
+    if constexpr (P == SW_EULER) {
+        __syncthreads();
+        tile_fix_bc<P, T>(p, rows, L, base);
+    }
+    __syncthreads();
+    if (q > 0) tile_down<P, T>(p, rows, L, W, base);
+    if (q == last) {
+        for (int x = threadIdx.x; x < W; x += blockDim.x)
+            state[wrap_pos(base + x, nx)] = tile_get<P, T>(rows, L, 0, x);
+        __syncthreads();
+    } else {
+        tile_up<P, T>(p, rows, L, W, base);
+        tile_export<P, T>(rows, L, W, slots + hl * W, slots + hr * W);
+        __threadfence();
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            st_release_u32(flags + hl, (unsigned)(q + 1));
+            st_release_u32(flags + hr, (unsigned)(q + 1));
+        }
+    }
+    return true;
+}
+
 template <int P, typename T>
 __global__ void __launch_bounds__(Scheme<P, T>::MAXT)
     k_persistent(const Params<T> p, typename Scheme<P, T>::G *__restrict__ state,
                  typename Scheme<P, T>::G *__restrict__ slots, unsigned *__restrict__ flags, int *status, const int W,
                  const int64_t n_diamonds) {
-    constexpr int R = Scheme<P, T>::R;
     extern __shared__ __align__(16) unsigned char sw_smem[];
     T *rows = reinterpret_cast<T *>(sw_smem);
-    const int L = W + 2 * R, h = W >> 1;
-    const int64_t nx = p.nx, nhalf = nx / h, ntile = nx / W;
-    const int64_t last = n_diamonds + 1;
+    const int64_t ntile = p.nx / W, last = n_diamonds + 1;
+    for (int64_t q = 0; q <= last; ++q)
+        for (int64_t t = blockIdx.x; t < ntile; t += gridDim.x)
+            if (!persistent_tile<P, T>(p, state, slots, flags, status, rows, W, q, last, t)) return;
+}
 
+// ------------------------------------------------------------ ensembles
+// Many independent domains of uneven length in one launch (BatchDev, in
+// sw_internal.h, maps a global tile to its domain).
+
+template <int P, typename T, int MODE>
+__global__ void __launch_bounds__(Scheme<P, T>::MAXT)
+    k_swept_batch(const Params<T> p, typename Scheme<P, T>::G *__restrict__ state,
+                  typename Scheme<P, T>::G *__restrict__ slots, const BatchDev b, const int W, const int phase) {
+    extern __shared__ __align__(16) unsigned char sw_smem[];
+    const int64_t g = blockIdx.x;
+    const int d = b.tile_dom[g];
+    const int64_t off = b.off[d];
+    Params<T> q = p;
+    q.nx = b.off[d + 1] - off;
+    swept_tile<P, T, MODE>(q, state + off, slots + 2 * off, reinterpret_cast<T *>(sw_smem), W, phase,
+                           g - b.tile0[d]);
+}
+
+template <int P, typename T>
+__global__ void __launch_bounds__(Scheme<P, T>::MAXT)
+    k_classic_batch(const Params<T> p, const typename Scheme<P, T>::G *__restrict__ in,
+                    typename Scheme<P, T>::G *__restrict__ out, const BatchDev b, const int sub) {
+    const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= b.n_cells) return;
+    int lo = 0, hi = b.n_dom;  // largest d with off[d] <= g
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (b.off[mid] <= g) lo = mid; else hi = mid;
+    }
+    const int64_t off = b.off[lo];
+    Params<T> q = p;
+    q.nx = b.off[lo + 1] - off;
+    classic_cell<P, T>(q, in + off, out + off, sub, g - off);
+}
+
+template <int P, typename T>
+__global__ void __launch_bounds__(Scheme<P, T>::MAXT)
+    k_persistent_batch(const Params<T> p, typename Scheme<P, T>::G *__restrict__ state,
+                       typename Scheme<P, T>::G *__restrict__ slots, const BatchDev b, unsigned *__restrict__ flags,
+                       int *status, const int W, const int64_t n_diamonds) {
+    extern __shared__ __align__(16) unsigned char sw_smem[];
+    T *rows = reinterpret_cast<T *>(sw_smem);
+    const int64_t last = n_diamonds + 1;
     for (int64_t q = 0; q <= last; ++q) {
-        const int phase = (int)(q & 1);
-        for (int64_t t = blockIdx.x; t < ntile; t += gridDim.x) {
-            const int64_t base = t * W + (int64_t)phase * h;
-            const int64_t hl = (2 * t + phase) % nhalf;
-            const int64_t hr = (hl + 1 == nhalf) ? 0 : hl + 1;
-            if (q == 0) {
-                for (int x = threadIdx.x; x < W; x += blockDim.x) tile_put<P, T>(rows, L, 0, x, state[base + x]);
-            } else {
-                if (!wait_slots(flags, hl, hr, (unsigned)q, status)) return;
-                tile_import_cg<P, T>(rows, L, W, slots + hl * W, slots + hr * W);
-            }
-            if constexpr (P == SW_EULER) {
-                __syncthreads();
-                tile_fix_bc<P, T>(p, rows, L, base);
-            }
-            __syncthreads();
-            if (q > 0) tile_down<P, T>(p, rows, L, W, base);
-            if (q == last) {
-                for (int x = threadIdx.x; x < W; x += blockDim.x)
-                    state[wrap_pos(base + x, nx)] = tile_get<P, T>(rows, L, 0, x);
-                __syncthreads();
-            } else {
-                tile_up<P, T>(p, rows, L, W, base);
-                tile_export<P, T>(rows, L, W, slots + hl * W, slots + hr * W);
-                __threadfence();
-                __syncthreads();
-                if (threadIdx.x == 0) {
-                    st_release_u32(flags + hl, (unsigned)(q + 1));
-                    st_release_u32(flags + hr, (unsigned)(q + 1));
-                }
-            }
+        for (int64_t g = blockIdx.x; g < b.n_tiles; g += gridDim.x) {
+            const int d = b.tile_dom[g];
+            const int64_t off = b.off[d];
+            Params<T> pp = p;
+            pp.nx = b.off[d + 1] - off;
+            if (!persistent_tile<P, T>(pp, state + off, slots + 2 * off, flags + 2 * b.tile0[d], status, rows, W, q,
+                                       last, g - b.tile0[d]))
+                return;
         }
     }
 }
@@ -172,6 +235,83 @@ cudaError_t launch_persistent(const void *vp, void *state, void *slots, unsigned
     int64_t nd = n_diamonds;
     void *args[] = {&p, &st, &sl, &flags, &status, &Wv, &nd};
     return cudaLaunchCooperativeKernel((const void *)kern, dim3((unsigned)grid), dim3(threads), args, smem, s);
+}
+
+template <int P, typename T>
+cudaError_t launch_swept_batch(const void *vp, int mode, int phase, void *state, void *slots, const void *bt, int W,
+                               int threads, cudaStream_t s) {
+    using G = typename Scheme<P, T>::G;
+    static bool configured = false;
+    if (!configured) {
+        allow_big_smem(k_swept_batch<P, T, MODE_UP>);
+        allow_big_smem(k_swept_batch<P, T, MODE_DIAMOND>);
+        allow_big_smem(k_swept_batch<P, T, MODE_DOWN>);
+        configured = true;
+    }
+    const Params<T> &p = *static_cast<const Params<T> *>(vp);
+    const BatchDev &b = *static_cast<const BatchDev *>(bt);
+    if (threads <= 0 || threads > Scheme<P, T>::MAXT) threads = W < Scheme<P, T>::MAXT ? W : Scheme<P, T>::MAXT;
+    const size_t smem = swept_smem_bytes<P, T>(W);
+    G *st = static_cast<G *>(state), *sl = static_cast<G *>(slots);
+    const unsigned grid = (unsigned)b.n_tiles;
+    switch (mode) {
+    case MODE_UP: k_swept_batch<P, T, MODE_UP><<<grid, threads, smem, s>>>(p, st, sl, b, W, phase); break;
+    case MODE_DIAMOND: k_swept_batch<P, T, MODE_DIAMOND><<<grid, threads, smem, s>>>(p, st, sl, b, W, phase); break;
+    default: k_swept_batch<P, T, MODE_DOWN><<<grid, threads, smem, s>>>(p, st, sl, b, W, phase); break;
+    }
+    return cudaGetLastError();
+}
+
+template <int P, typename T>
+cudaError_t launch_classic_batch(const void *vp, const void *in, void *out, int sub, const void *bt, int block,
+                                 cudaStream_t s) {
+    using G = typename Scheme<P, T>::G;
+    const Params<T> &p = *static_cast<const Params<T> *>(vp);
+    const BatchDev &b = *static_cast<const BatchDev *>(bt);
+    if (block <= 0 || block > Scheme<P, T>::MAXT) block = 256;
+    const int64_t grid = (b.n_cells + block - 1) / block;
+    k_classic_batch<P, T><<<(unsigned)grid, block, 0, s>>>(p, static_cast<const G *>(in), static_cast<G *>(out), b,
+                                                            sub);
+    return cudaGetLastError();
+}
+
+// Cooperative launch through cudaLaunchKernelEx so that it can be captured
+// into a CUDA graph.
+template <int P, typename T>
+cudaError_t launch_persistent_batch(const void *vp, void *state, void *slots, const void *bt, unsigned *flags,
+                                    int *status, int W, int threads, int64_t n_diamonds, cudaStream_t s) {
+    using G = typename Scheme<P, T>::G;
+    static bool configured = false;
+    auto kern = k_persistent_batch<P, T>;
+    const size_t smem = swept_smem_bytes<P, T>(W);
+    if (!configured) {
+        allow_big_smem(kern);
+        configured = true;
+    }
+    if (threads <= 0 || threads > Scheme<P, T>::MAXT) threads = W < Scheme<P, T>::MAXT ? W : Scheme<P, T>::MAXT;
+    const BatchDev &b = *static_cast<const BatchDev *>(bt);
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) return cudaErrorInvalidConfiguration;
+    int64_t grid = (int64_t)per_sm * sms;
+    if (grid > b.n_tiles) grid = b.n_tiles;
+    e = cudaMemsetAsync(flags, 0, sizeof(unsigned) * 2 * b.n_tiles, s);
+    if (e != cudaSuccess) return e;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(threads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kern, *static_cast<const Params<T> *>(vp), static_cast<G *>(state),
+                              static_cast<G *>(slots), b, flags, status, W, n_diamonds);
 }
 
 }  // namespace sw

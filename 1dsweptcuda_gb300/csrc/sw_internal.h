@@ -23,6 +23,18 @@ struct Params {
     int pow2;                  // KS: c4, d2, d4 are exact powers of two (products by them are exact)
 };
 
+// Device tables of an ensemble (see sw_run_batch): domain d holds cells
+// [off[d], off[d+1]), its slots are the same range times two, its flags
+// [2*tile0[d], ...); tile_dom maps a global tile of width W to its domain.
+struct BatchDev {
+    const int32_t *tile_dom;
+    const int64_t *off;    // n_dom + 1 cell offsets
+    const int64_t *tile0;  // first global tile of each domain
+    int64_t n_tiles;
+    int64_t n_cells;
+    int32_t n_dom;
+};
+
 // Swept launch modes.
 enum SweptMode { MODE_UP = 0, MODE_DIAMOND = 1, MODE_DOWN = 2 };
 
@@ -50,6 +62,13 @@ struct Ops {
     cudaError_t (*unpack)(const void *in4, void *out3, int64_t nx, cudaStream_t s);
     // dynamic shared memory a swept block of width W needs
     size_t (*swept_smem)(int W);
+    // ensembles: `batch` points at a BatchDev (device tables), `threads` per block (0 = W)
+    cudaError_t (*batch_swept)(const void *params, int mode, int phase, void *state, void *slots, const void *batch,
+                               int W, int threads, cudaStream_t s);
+    cudaError_t (*batch_classic)(const void *params, const void *in, void *out, int sub, const void *batch, int block,
+                                 cudaStream_t s);
+    cudaError_t (*batch_persistent)(const void *params, void *state, void *slots, const void *batch, unsigned *flags,
+                                    int *status, int W, int threads, int64_t n_diamonds, cudaStream_t s);
 };
 
 const Ops *heat_ops(int prec);

@@ -27,7 +27,8 @@ ERRORS = {0: "SW_OK", -1: "SW_ERR_ARG", -2: "SW_ERR_SIZE", -3: "SW_ERR_UNSTABLE"
 
 EXPORTED = ["sw_abi_version", "sw_strerror", "sw_ctx_create", "sw_ctx_destroy", "sw_ctx_last_error",
             "sw_config_init", "sw_validate", "sw_constants_of", "sw_initial_condition", "sw_run",
-            "sw_run_device", "sw_plan", "sw_cli_main"]
+            "sw_run_device", "sw_plan", "sw_cli_main", "sw_run_batch", "sw_run_batch_device",
+            "sw_query_tuning"]
 
 
 class Config(C.Structure):
@@ -37,6 +38,7 @@ class Config(C.Structure):
         ("dt", C.c_double), ("tf", C.c_double), ("freq", C.c_double), ("n_steps", C.c_int64),
         ("dx", C.c_double), ("alpha", C.c_double), ("gamma", C.c_double),
         ("left", C.c_double * 3), ("right", C.c_double * 3),
+        ("threads", C.c_int32), ("reserved", C.c_int32),
     ]
 
 
@@ -63,6 +65,15 @@ class Result(C.Structure):
 class PlanInfo(C.Structure):
     _fields_ = [("t_final", C.c_double), ("n_steps", C.c_int64), ("n_snapshots", C.c_int32),
                 ("tile", C.c_int32), ("launches", C.c_int64)]
+
+
+class Tuning(C.Structure):
+    _fields_ = [("tile", C.c_int32), ("threads", C.c_int32), ("cell_updates_per_s", C.c_double),
+                ("n_candidates", C.c_int32), ("cand_tile", C.c_int32 * 48), ("cand_threads", C.c_int32 * 48),
+                ("cand_rate", C.c_double * 48)]
+
+    def candidates(self) -> list[tuple[int, int, float]]:
+        return [(self.cand_tile[i], self.cand_threads[i], self.cand_rate[i]) for i in range(self.n_candidates)]
 
 
 SNAPSHOT_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_double, C.c_void_p, C.c_int64)
@@ -106,8 +117,13 @@ def library():
     L.sw_run_device.argtypes = [C.c_void_p, cp, C.c_void_p, C.c_void_p, rp]
     L.sw_cli_main.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_char_p)]
     L.sw_plan.argtypes = [cp, C.POINTER(PlanInfo), C.POINTER(C.c_double), C.POINTER(C.c_int64), C.c_int32]
+    i64p = C.POINTER(C.c_int64)
+    L.sw_run_batch.argtypes = [C.c_void_p, cp, C.c_int32, i64p, C.c_void_p, C.c_void_p, rp]
+    L.sw_run_batch_device.argtypes = [C.c_void_p, cp, C.c_int32, i64p, C.c_void_p, C.c_void_p, rp]
+    L.sw_query_tuning.argtypes = [C.c_void_p, cp, C.c_int32, i64p, C.POINTER(Tuning)]
     for name in ("sw_ctx_create", "sw_ctx_destroy", "sw_config_init", "sw_validate", "sw_constants_of",
-                 "sw_initial_condition", "sw_run", "sw_run_device", "sw_cli_main", "sw_plan"):
+                 "sw_initial_condition", "sw_run", "sw_run_device", "sw_cli_main", "sw_plan", "sw_run_batch",
+                 "sw_run_batch_device", "sw_query_tuning"):
         getattr(L, name).restype = C.c_int
     _lib = L
     return L
@@ -223,6 +239,49 @@ class Solver:
         if rc:
             raise self._err(rc, "sw_run_device")
         return res
+
+
+def _nx_array(nx):
+    arr = np.ascontiguousarray(nx, dtype=np.int64)
+    return arr, arr.ctypes.data_as(C.POINTER(C.c_int64))
+
+
+class _BatchMixin:
+    def run_batch(self, cfg: Config, nx, ic: np.ndarray) -> tuple[np.ndarray, Result]:
+        """sw_run_batch: the domains' states concatenated (host layout) in, out."""
+        arr, ptr = _nx_array(nx)
+        n = int(arr.sum()) * COMPONENTS[cfg.problem]
+        ic = np.ascontiguousarray(ic, dtype=_dtype(cfg))
+        if ic.size != n:
+            raise ValueError("ensemble state has %d values, expected %d" % (ic.size, n))
+        out = np.empty_like(ic)
+        res = Result()
+        rc = self._lib.sw_run_batch(self._ctx, C.byref(cfg), len(arr), ptr, ic.ctypes.data, out.ctypes.data,
+                                    C.byref(res))
+        if rc:
+            raise self._err(rc, "sw_run_batch")
+        return out, res
+
+    def run_batch_device(self, cfg: Config, nx, state_ptr: int, stream: int = 0) -> Result:
+        arr, ptr = _nx_array(nx)
+        res = Result()
+        rc = self._lib.sw_run_batch_device(self._ctx, C.byref(cfg), len(arr), ptr, C.c_void_p(state_ptr),
+                                           C.c_void_p(stream) if stream else None, C.byref(res))
+        if rc:
+            raise self._err(rc, "sw_run_batch_device")
+        return res
+
+    def tune(self, cfg: Config, nx) -> "Tuning":
+        arr, ptr = _nx_array(nx)
+        t = Tuning()
+        rc = self._lib.sw_query_tuning(self._ctx, C.byref(cfg), len(arr), ptr, C.byref(t))
+        if rc:
+            raise self._err(rc, "sw_query_tuning")
+        return t
+
+
+for _name in ("run_batch", "run_batch_device", "tune"):
+    setattr(Solver, _name, getattr(_BatchMixin, _name))
 
 
 def plan(cfg: Config, cap: int = 4096):

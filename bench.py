@@ -45,6 +45,9 @@ DP_OPS_PER_UPDATE = 30    # FP64 instructions per cell-update: 2 sub-steps x 15 
 # probe: 0.600e12 DFMA/s (2.06 per clock per SM at 1.92 GHz; 1.2 TFLOP/s).
 FP64_OPS_PEAK = 0.600e12
 BASELINE_K40_KS_F64_SWEPT = 1.07e10  # KS FP64 swept, nx=2^20, K40c
+# DRAM bytes (read + write) of one diamond launch of this workload from one ncu
+# capture (profiles/ks_f64_swept_diamond_nx2e20.md; cold-cache replay).
+DIAMOND_TRAFFIC_BYTES = 16798720
 
 
 def _peaks():
@@ -273,7 +276,8 @@ def run_ours(args) -> None:
     achieved = alg_bytes / (launch_ms * 1e-3) / 1e9
     roof = {"bound": "hbm", "kernel": "k_swept<KS,double,DIAMOND>", "achieved": achieved, "peak": hbm,
             "unit": "GB/s", "frac": achieved / hbm, "peak_source": peak_src,
-            "traffic": None, "launch_ms": launch_ms,
+            "traffic": DIAMOND_TRAFFIC_BYTES, "traffic_source": "ncu dram__bytes_read+write, one diamond launch",
+            "launch_ms": launch_ms,
             "algorithmic_bytes_per_launch": alg_bytes,
             "note": "effective bandwidth: classic KS FP64 bytes (40 B/cell-update) x cells x 32 steps per "
                     "diamond launch; the swept kernel's real DRAM traffic is far lower, its bound is the FP64 pipe"}

@@ -91,6 +91,8 @@ typedef struct sw_config {
     double gamma;        /* Euler heat-capacity ratio 1.4 */
     double left[3];      /* Euler left state (rho, u, p); all 0 = Sod (1, 0, 1) */
     double right[3];     /* Euler right state (rho, u, p); all 0 = Sod (0.125, 0, 0.1) */
+    int32_t threads;     /* ensembles: threads per swept block (0 = one per cell, capped at the kernel's limit) */
+    int32_t reserved;
 } sw_config;
 
 /* Derived constants, rounded to the run's precision exactly as the
@@ -173,6 +175,36 @@ typedef struct sw_plan_info {
     int64_t launches;    /* kernel launches the run will issue (launch-per-pass paths) */
 } sw_plan_info;
 int sw_plan(const sw_config *cfg, sw_plan_info *out, double *snap_t, int64_t *snap_steps, int32_t cap);
+
+/* ---------------------------------------------------------- ensembles
+ * No counterpart in the reference, which solves one domain per program run:
+ * many independent domains of uneven length advanced together, in one launch
+ * per swept pass (alg 1) or one persistent cooperative launch (alg 2), the
+ * whole sequence captured in a CUDA graph and replayed while the shape is
+ * unchanged.  cfg->time_mode must be SW_TIME_STEPS; cfg->nx is ignored, the
+ * domain lengths are nx[0..n_domains-1]; cfg->tpb is the tile width (it must
+ * divide every domain; 0 = take the autotuner's choice) and cfg->threads the
+ * threads per block.  State: the domains concatenated in order, in the host
+ * (sw_run_batch) or device (sw_run_batch_device) layout. */
+typedef struct sw_tuning {
+    int32_t tile;                 /* chosen tile width; a swept cycle is tile/(R*S) time steps */
+    int32_t threads;              /* chosen threads per block */
+    double cell_updates_per_s;    /* measured rate of the choice */
+    int32_t n_candidates;
+    int32_t cand_tile[48];
+    int32_t cand_threads[48];
+    double cand_rate[48];
+} sw_tuning;
+
+int sw_run_batch(sw_ctx *ctx, const sw_config *cfg, int32_t n_domains, const int64_t *nx, const void *ic_host,
+                 void *final_host, sw_result *out);
+int sw_run_batch_device(sw_ctx *ctx, const sw_config *cfg, int32_t n_domains, const int64_t *nx, void *state_dev,
+                        void *stream, sw_result *out);
+/* Autotuner: times every valid (tile width, threads per block) pair on a
+ * sample of the ensemble (every k-th domain, at least 2^22 cells where there
+ * are that many) for the same number of time steps, and returns the fastest.
+ * The choice is remembered by the context for this ensemble shape. */
+int sw_query_tuning(sw_ctx *ctx, const sw_config *cfg, int32_t n_domains, const int64_t *nx, sw_tuning *out);
 
 /* The whole program: argv exactly as bin/<Problem><Precision>Out takes it
  * (replaces main(), Heat1D_SweptShared.cu:697-836, KS1D_SweptShared.cu:866-1029,

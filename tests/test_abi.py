@@ -46,7 +46,7 @@ def test_struct_layouts_match_header(sw, tmp_path):
     native = import_module("1dsweptcuda_gb300.native")
     src = tmp_path / "l.c"
     fields = {"sw_config": native.Config, "sw_constants": native.Constants, "sw_result": native.Result,
-              "sw_plan_info": native.PlanInfo}
+              "sw_plan_info": native.PlanInfo, "sw_tuning": native.Tuning}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "swept1d.h"', "int main(void){"]
     for cname, py in fields.items():
         lines.append('printf("%s %%zu\\n", sizeof(%s));' % (cname, cname))
@@ -153,3 +153,20 @@ def test_plan_exact_steps(sw):
     cfg = sw.make_config(1, 8, alg=1, nx=1 << 20, tpb=256, dt=0.005, time_mode=sw.TIME_STEPS, n_steps=40000)
     info, _, _ = sw.plan(cfg)
     assert info.launches == 40000 // 32 + 1 and info.tile == 256  # up + 1249 diamonds + down
+
+
+def test_ensemble_generator():
+    """The ensemble workload: log-uniform nx in 2^10..2^16 (mean ~18.6k), 8 modes with N(0,1)/k amplitudes."""
+    from importlib import import_module
+    ens = import_module("1dsweptcuda_gb300.ensemble")
+    nx, u = ens.make_ensemble(n_domains=4096)
+    e = np.log2(nx).astype(int)
+    assert e.min() == 10 and e.max() == 16 and set(np.unique(e)) == set(range(10, 17))
+    assert 17000 < nx.mean() < 20000
+    assert u.size == nx.sum() and np.isfinite(u).all()
+    parts = ens.split(u, nx)
+    assert [len(p) for p in parts] == list(nx)
+    # each domain is a trigonometric polynomial of its own period: zero mean
+    assert max(abs(float(p.mean())) for p in parts[:50]) < 1e-9
+    nx2, u2 = ens.make_ensemble(n_domains=4096)
+    assert (nx2 == nx).all() and np.array_equal(u2, u)   # seeded
