@@ -28,7 +28,8 @@ ERRORS = {0: "SW_OK", -1: "SW_ERR_ARG", -2: "SW_ERR_SIZE", -3: "SW_ERR_UNSTABLE"
 EXPORTED = ["sw_abi_version", "sw_strerror", "sw_ctx_create", "sw_ctx_destroy", "sw_ctx_last_error",
             "sw_config_init", "sw_validate", "sw_constants_of", "sw_initial_condition", "sw_run",
             "sw_run_device", "sw_plan", "sw_cli_main", "sw_run_batch", "sw_run_batch_device",
-            "sw_query_tuning"]
+            "sw_query_tuning", "sw_run_device_noalloc"]
+NOALLOC_SCRATCH_BYTES = 24 * 1024 * 1024
 
 
 class Config(C.Structure):
@@ -121,9 +122,10 @@ def library():
     L.sw_run_batch.argtypes = [C.c_void_p, cp, C.c_int32, i64p, C.c_void_p, C.c_void_p, rp]
     L.sw_run_batch_device.argtypes = [C.c_void_p, cp, C.c_int32, i64p, C.c_void_p, C.c_void_p, rp]
     L.sw_query_tuning.argtypes = [C.c_void_p, cp, C.c_int32, i64p, C.POINTER(Tuning)]
+    L.sw_run_device_noalloc.argtypes = [cp, C.c_void_p, C.c_void_p]
     for name in ("sw_ctx_create", "sw_ctx_destroy", "sw_config_init", "sw_validate", "sw_constants_of",
                  "sw_initial_condition", "sw_run", "sw_run_device", "sw_cli_main", "sw_plan", "sw_run_batch",
-                 "sw_run_batch_device", "sw_query_tuning"):
+                 "sw_run_batch_device", "sw_query_tuning", "sw_run_device_noalloc"):
         getattr(L, name).restype = C.c_int
     _lib = L
     return L
@@ -282,6 +284,15 @@ class _BatchMixin:
 
 for _name in ("run_batch", "run_batch_device", "tune"):
     setattr(Solver, _name, getattr(_BatchMixin, _name))
+
+
+def run_device_noalloc(cfg: Config, state_ptr: int, stream: int = 0) -> None:
+    """sw_run_device_noalloc: swept run on a device state using the library's
+    fixed scratch array (no device allocation); enqueued on `stream`, returns
+    without waiting."""
+    rc = library().sw_run_device_noalloc(C.byref(cfg), C.c_void_p(state_ptr), C.c_void_p(stream) if stream else None)
+    if rc:
+        raise NativeError(rc, "sw_run_device_noalloc")
 
 
 def plan(cfg: Config, cap: int = 4096):

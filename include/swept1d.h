@@ -206,6 +206,34 @@ int sw_run_batch_device(sw_ctx *ctx, const sw_config *cfg, int32_t n_domains, co
  * The choice is remembered by the context for this ensemble shape. */
 int sw_query_tuning(sw_ctx *ctx, const sw_config *cfg, int32_t n_domains, const int64_t *nx, sw_tuning *out);
 
+/* ------------------------------------------------ no-allocation entry point
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory when they step the solver: codes that size all GPU memory once at
+ * start-up and own it through their own arena or pool, and code that runs
+ * where cudaMalloc is not allowed or would stall the device (a real-time
+ * loop, a region another library has locked down).  sw_run_device needs a
+ * context whose buffers grow on demand; this call needs none.
+ *
+ * It runs the swept path (cfg->alg must be SW_ALG_SWEPT, cfg->time_mode
+ * SW_TIME_STEPS) on the caller's device-resident state (device layout, see
+ * sw_run_device), enqueued on `stream` (a cudaStream_t, NULL = legacy default
+ * stream), and returns without waiting.  Its scratch -- the edge slots, two
+ * cells per cell, and one work row for the classic remainder steps, so three
+ * times the state's bytes -- is a fixed device array of
+ * SW_NOALLOC_SCRATCH_BYTES (24 MiB) inside the library, held by every GPU that
+ * loads it until the process exits; larger states return SW_ERR_SIZE
+ * (e.g. up to nx = 2^20 for FP64 Heat/KS, 2^18 for FP64 Euler).  It calls no
+ * cudaMalloc, cudaFree or other allocating routine.
+ *
+ * The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * Every call on a device shares the one array and leaves its contents behind
+ * (nothing in it needs to start at zero); calls that overlap on the GPU --
+ * on different streams, or from different host threads -- race on it, so
+ * order them on one stream. */
+#define SW_NOALLOC_SCRATCH_BYTES (24u * 1024u * 1024u)
+int sw_run_device_noalloc(const sw_config *cfg, void *state_dev, void *stream);
+
 /* The whole program: argv exactly as bin/<Problem><Precision>Out takes it
  * (replaces main(), Heat1D_SweptShared.cu:697-836, KS1D_SweptShared.cu:866-1029,
  * Euler1D_SweptShared.cu:1112-1287).  Writes solution.dat and appends the
