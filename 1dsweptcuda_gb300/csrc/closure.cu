@@ -1,0 +1,570 @@
+// KS closure network: a 3-layer 1D convolution (1 -> 32 -> 32 -> 1 channels,
+// kernel 5, GELU, circular padding per domain) that corrects a coarse KS step.
+// Parameters are FP32 masters rounded to BF16 for the forward pass.  The
+// 32 -> 32 layer -- 94 % of the work -- runs on the tensor cores
+// (mma.sync.m16n8k16, BF16 operands, FP32 accumulation) forward and backward;
+// the 1 -> 32 and 32 -> 1 layers run in FP32 on the CUDA cores with the
+// BF16-rounded weights.  oracle/closure.py restates the same arithmetic.
+//
+// Tiles: a block produces TOUT = 128 consecutive outputs of one domain.  In
+// tile coordinates (x0 = first output):
+//   us[j] = u[x0 - 6 + j],        j < 152
+//   a1[r] : position x0 - 4 + r,  r < 148  (z1 = w1 * us[r .. r+4] + b1)
+//   z2[p] : position x0 - 2 + p,  p < 144  (needs a1[p .. p+4]; p < 132 used)
+//   d[q]  : position x0 + q,      q < 128  (needs a2[q .. q+4])
+// The im2col of layer 2 is free: the A fragment of tap t is the a1 rows
+// shifted by t.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+#include "ctx.h"
+#include "stencils.cuh"
+#include "sw_internal.h"
+
+namespace sw {
+namespace cl {
+
+constexpr int CH = 32, KW = 5;
+constexpr int TOUT = 128;
+constexpr int NU = TOUT + 24;   // 152 input cells
+constexpr int NA1 = TOUT + 20;  // 148 a1 rows
+constexpr int NZ2 = 144;        // 9 m-tiles of 16 rows
+constexpr int NA2 = TOUT + 4;   // 132 a2 rows used
+constexpr int LDB = 40;         // bf16 row stride (80 B: conflict-free fragment reads)
+constexpr int LDF = 33;         // fp32 row stride
+constexpr int THREADS = 256;
+// parameter offsets (flat FP32 vector); the last value is the output scale s
+// (delta = s * net(u)), fixed by the caller and left alone by training
+constexpr int OW1 = 0, OB1 = 160, OW2 = 192, OB2 = 5312, OW3 = 5344, OB3 = 5504, OSCALE = 5505;
+constexpr int NTRAIN = 5505, NPARAM = 5506;
+
+__device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f)); }
+__device__ __forceinline__ float gelu_grad(float x) {
+    return 0.5f * (1.0f + erff(x * 0.70710678118654752f)) + x * 0.39894228040143268f * expf(-0.5f * x * x);
+}
+__device__ __forceinline__ float bf16r(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
+__device__ __forceinline__ uint32_t pack2(__nv_bfloat16 lo, __nv_bfloat16 hi) {
+    return (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
+}
+__device__ __forceinline__ uint32_t ld2(const __nv_bfloat16 *p) { return *reinterpret_cast<const uint32_t *>(p); }
+
+// D = A * B + D, m16n8k16, A row-major BF16, B column-major BF16, FP32 accumulate
+__device__ __forceinline__ void mma_bf16(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3, uint32_t b0,
+                                         uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+struct Smem {
+    float us[NU];
+    float w1[CH * KW], b1[CH], b2[CH], w3[CH * KW], b3, scale;
+    __nv_bfloat16 a1[NA1 * LDB];            // layer-1 activations, BF16 (the MMA A operand)
+    __nv_bfloat16 w2[KW * CH * LDB];        // w2[t][o][i], i contiguous (the MMA B operand)
+    float z2[NA2 * LDF];                    // layer-2 pre-activations
+    float a2[NA2 * LDF];                    // layer-2 activations gelu(z2)
+    float z1[NA1 * LDF];                    // layer-1 pre-activations (backward only)
+};
+
+// Load the tile's inputs (periodic within the domain) and the weights.
+__device__ void load_tile(Smem &s, const float *__restrict__ theta, const float *__restrict__ u, int64_t n,
+                          int64_t x0) {
+    for (int j = threadIdx.x; j < NU; j += blockDim.x) {
+        int64_t q = x0 - 6 + j;
+        q %= n;
+        if (q < 0) q += n;
+        s.us[j] = u[q];
+    }
+    for (int i = threadIdx.x; i < CH * KW; i += blockDim.x) {
+        s.w1[i] = bf16r(theta[OW1 + i]);
+        s.w3[i] = bf16r(theta[OW3 + i]);
+    }
+    for (int i = threadIdx.x; i < CH; i += blockDim.x) {
+        s.b1[i] = theta[OB1 + i];
+        s.b2[i] = theta[OB2 + i];
+    }
+    if (threadIdx.x == 0) {
+        s.b3 = theta[OB3];
+        s.scale = theta[OSCALE];
+    }
+    // w2 flat is [o][i][t]; smem is [t][o][i]
+    for (int k = threadIdx.x; k < CH * CH * KW; k += blockDim.x) {
+        const int o = k / (CH * KW), i = (k / KW) % CH, t = k % KW;
+        s.w2[(t * CH + o) * LDB + i] = __float2bfloat16_rn(theta[OW2 + k]);
+    }
+}
+
+// Layers 1 and 2 of the forward pass: a1 (BF16), z2 and a2 = gelu(z2) (FP32).
+// Requires load_tile and a barrier first.
+__device__ void forward_12(Smem &s, bool keep_z1) {
+    for (int k = threadIdx.x; k < NA1 * CH; k += blockDim.x) {
+        const int r = k / CH, o = k % CH;
+        float z = s.b1[o];
+#pragma unroll
+        for (int t = 0; t < KW; ++t) z = fmaf(s.w1[o * KW + t], s.us[r + t], z);
+        if (keep_z1) s.z1[r * LDF + o] = z;
+        s.a1[r * LDB + o] = __float2bfloat16_rn(gelu(z));
+    }
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, q = lane & 3;
+    for (int m = warp; m < NZ2 / 16; m += blockDim.x >> 5) {
+        const int p0 = m * 16;
+        float acc[4][4] = {};
+#pragma unroll
+        for (int t = 0; t < KW; ++t) {
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                // rows beyond NA1 are only reached for p >= NA2 (discarded rows): clamp the read
+                const int ra = min(p0 + g + t, NA1 - 1), rb = min(p0 + g + 8 + t, NA1 - 1);
+                const uint32_t a0 = ld2(&s.a1[ra * LDB + 16 * h + 2 * q]);
+                const uint32_t a1 = ld2(&s.a1[rb * LDB + 16 * h + 2 * q]);
+                const uint32_t a2 = ld2(&s.a1[ra * LDB + 16 * h + 8 + 2 * q]);
+                const uint32_t a3 = ld2(&s.a1[rb * LDB + 16 * h + 8 + 2 * q]);
+#pragma unroll
+                for (int nt = 0; nt < 4; ++nt) {
+                    const __nv_bfloat16 *wb = &s.w2[(t * CH + nt * 8 + g) * LDB + 16 * h];
+                    mma_bf16(acc[nt], a0, a1, a2, a3, ld2(wb + 2 * q), ld2(wb + 8 + 2 * q));
+                }
+            }
+        }
+#pragma unroll
+        for (int nt = 0; nt < 4; ++nt) {
+            const int o = nt * 8 + 2 * q;
+            const int r0 = p0 + g, r1 = p0 + g + 8;
+            if (r0 < NA2) {
+                const float z0 = acc[nt][0] + s.b2[o], z1 = acc[nt][1] + s.b2[o + 1];
+                s.z2[r0 * LDF + o] = z0;
+                s.z2[r0 * LDF + o + 1] = z1;
+                s.a2[r0 * LDF + o] = gelu(z0);
+                s.a2[r0 * LDF + o + 1] = gelu(z1);
+            }
+            if (r1 < NA2) {
+                const float z2 = acc[nt][2] + s.b2[o], z3 = acc[nt][3] + s.b2[o + 1];
+                s.z2[r1 * LDF + o] = z2;
+                s.z2[r1 * LDF + o + 1] = z3;
+                s.a2[r1 * LDF + o] = gelu(z2);
+                s.a2[r1 * LDF + o + 1] = gelu(z3);
+            }
+        }
+    }
+    __syncthreads();
+}
+
+// Layer 3 for output q: b3 + sum_{t,i} w3[i][t] * a2[q + t][i].
+__device__ __forceinline__ float layer3(const Smem &s, int q) {
+    float d = 0.0f;
+#pragma unroll
+    for (int t = 0; t < KW; ++t)
+#pragma unroll 8
+        for (int i = 0; i < CH; ++i) d = fmaf(s.w3[i * KW + t], s.a2[(q + t) * LDF + i], d);
+    return d + s.b3;
+}
+
+// ---------------------------------------------------------------- kernels
+// delta = f(u) for every cell of n_dom domains of n cells (n a multiple of TOUT).
+__global__ void __launch_bounds__(THREADS) k_infer(const float *__restrict__ theta, const float *__restrict__ u,
+                                                   float *__restrict__ delta, int64_t n, int64_t tiles_per_dom) {
+    extern __shared__ __align__(16) unsigned char raw[];
+    Smem &s = *reinterpret_cast<Smem *>(raw);
+    const int64_t dom = blockIdx.x / tiles_per_dom, x0 = (blockIdx.x % tiles_per_dom) * TOUT;
+    const float *ud = u + dom * n;
+    load_tile(s, theta, ud, n, x0);
+    __syncthreads();
+    forward_12(s, false);
+    for (int q = threadIdx.x; q < TOUT; q += blockDim.x) delta[dom * n + x0 + q] = s.scale * layer3(s, q);
+}
+
+// One coarse KS step fused with the closure: u_out = classic KS step(u_in) + f(u_in).
+// The KS predictor/corrector reads u_in on [x0-4, x0+TOUT+4) from the same tile.
+__global__ void __launch_bounds__(THREADS) k_step(const float *__restrict__ theta, const Params<float> pk,
+                                                  const float *__restrict__ u, float *__restrict__ out, int64_t n,
+                                                  int64_t tiles_per_dom, int use_closure) {
+    extern __shared__ __align__(16) unsigned char raw[];
+    Smem &s = *reinterpret_cast<Smem *>(raw);
+    const int64_t dom = blockIdx.x / tiles_per_dom, x0 = (blockIdx.x % tiles_per_dom) * TOUT;
+    load_tile(s, theta, u + dom * n, n, x0);
+    __syncthreads();
+    if (use_closure) forward_12(s, false);
+    // predictor on positions x0-2 .. x0+TOUT+1 (us index 4 .. TOUT+7), kept in z1 scratch (column 0)
+    for (int j = threadIdx.x; j < TOUT + 4; j += blockDim.x) {
+        const int c = j + 4;
+        s.z1[j * LDF] = ks_predict(pk, s.us[c - 2], s.us[c - 1], s.us[c], s.us[c + 1], s.us[c + 2]);
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < TOUT; q += blockDim.x) {
+        const int c = q + 6, j = q + 2;  // us index of x0+q; predictor index of x0+q
+        float v = ks_correct(pk, s.us[c], s.z1[(j - 2) * LDF], s.z1[(j - 1) * LDF], s.z1[j * LDF],
+                             s.z1[(j + 1) * LDF], s.z1[(j + 2) * LDF]);
+        if (use_closure) v += s.scale * layer3(s, q);
+        out[dom * n + x0 + q] = v;
+    }
+}
+
+// Loss and parameter gradients (forward + backward), summed over the tiles a
+// block visits into its row of `partial` ([gridDim.x][NPARAM + 1], last = loss).
+// The loss is on the scaled defect: L = wpt * sum (net(u) - target / s)^2,
+// wpt = 1 / (points in the batch), s the output scale.
+__global__ void __launch_bounds__(THREADS) k_grad(const float *__restrict__ theta, const float *__restrict__ u,
+                                                  const float *__restrict__ target, const int64_t *__restrict__ rows,
+                                                  float *__restrict__ partial, int64_t n, int64_t tiles_per_dom,
+                                                  int64_t n_tiles, float scale) {
+    extern __shared__ __align__(16) unsigned char raw[];
+    Smem &s = *reinterpret_cast<Smem *>(raw);
+    __shared__ float g[NPARAM + 1];                 // this block's sums of the small-layer gradients and the loss
+    __shared__ float dd[TOUT];                      // dL/ddelta
+    __shared__ __nv_bfloat16 dzT[CH * (NZ2 + 8)];   // dz2 as [o][p] (BF16), p contiguous, for dW2
+    __shared__ __nv_bfloat16 dzP[(NZ2 + 8) * LDB];  // dz2 as [4 + p][o] (BF16), 4 zero rows in front, for da1
+    for (int i = threadIdx.x; i < NPARAM + 1; i += blockDim.x) g[i] = 0.0f;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, gq = lane >> 2, q4 = lane & 3;
+    const int nwarp = blockDim.x >> 5;
+    // dW2 accumulators: warp w owns (m-tile mo, n-tile nn) pairs k = w, w+8, ... of 2 x 20
+    float accw[5][4] = {};
+    __syncthreads();
+
+    for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+        const int64_t b = tile / tiles_per_dom, x0 = (tile % tiles_per_dom) * TOUT;
+        const int64_t dom = rows ? rows[b] : b;  // minibatch row -> sample
+        load_tile(s, theta, u + dom * n, n, x0);
+        __syncthreads();
+        forward_12(s, true);
+        // delta, dL/ddelta, loss, dW3, db3
+        for (int q = threadIdx.x; q < TOUT; q += blockDim.x) {
+            const float d = layer3(s, q);
+            const float e = d - target[dom * n + x0 + q] / s.scale;
+            dd[q] = 2.0f * scale * e;
+            atomicAdd(&g[NPARAM], scale * e * e);
+        }
+        __syncthreads();
+        for (int k = threadIdx.x; k < CH * KW; k += blockDim.x) {
+            const int i = k / KW, t = k % KW;
+            float a = 0.0f;
+            for (int q = 0; q < TOUT; ++q) a = fmaf(dd[q], s.a2[(q + t) * LDF + i], a);
+            g[OW3 + k] += a;
+        }
+        if (threadIdx.x < 32) {
+            float a = 0.0f;
+            for (int q = threadIdx.x; q < TOUT; q += 32) a += dd[q];
+#pragma unroll
+            for (int off = 16; off; off >>= 1) a += __shfl_xor_sync(0xffffffffu, a, off);
+            if (threadIdx.x == 0) g[OB3] += a;
+        }
+        // dz2[p][o] = (sum_t w3[o][t] dd[p - t]) * gelu'(z2[p][o]), p < NA2; zero beyond
+        for (int k = threadIdx.x; k < (NZ2 + 8) * CH; k += blockDim.x) {
+            const int p = k / CH, o = k % CH;
+            float v = 0.0f;
+            if (p < NA2) {
+                float da = 0.0f;
+#pragma unroll
+                for (int t = 0; t < KW; ++t) {
+                    const int qq = p - t;
+                    if (qq >= 0 && qq < TOUT) da = fmaf(s.w3[o * KW + t], dd[qq], da);
+                }
+                v = da * gelu_grad(s.z2[p * LDF + o]);
+            }
+            const __nv_bfloat16 b = __float2bfloat16_rn(v);
+            dzT[o * (NZ2 + 8) + p] = b;
+            if (p + 4 < NZ2 + 8) dzP[(p + 4) * LDB + o] = b;
+            if (p < 4) dzP[p * LDB + o] = __float2bfloat16_rn(0.0f);
+        }
+        __syncthreads();
+        // db2
+        for (int o = threadIdx.x; o < CH; o += blockDim.x) {
+            float a = 0.0f;
+            for (int p = 0; p < NA2; ++p) a += __bfloat162float(dzT[o * (NZ2 + 8) + p]);
+            g[OB2 + o] += a;
+        }
+        // dW2[o][(t,i)] += sum_p dz2[p][o] a1[p + t][i]: M = o (2 tiles), N = (t, i) (20 tiles), K = p (9 steps)
+#pragma unroll
+        for (int slot = 0; slot < 5; ++slot) {
+            const int k = warp + slot * 8;  // 8 warps x 5 slots = 40 (m-tile, n-tile) pairs
+            const int mo = k / 20, nn = k % 20, t = nn / 4, i0 = (nn % 4) * 8;
+            for (int ks = 0; ks < NZ2 / 16; ++ks) {
+                const int p0 = ks * 16;
+                const __nv_bfloat16 *ra = &dzT[(mo * 16 + gq) * (NZ2 + 8) + p0];
+                const __nv_bfloat16 *rb = &dzT[(mo * 16 + gq + 8) * (NZ2 + 8) + p0];
+                const uint32_t a0 = ld2(ra + 2 * q4), a1 = ld2(rb + 2 * q4);
+                const uint32_t a2 = ld2(ra + 8 + 2 * q4), a3 = ld2(rb + 8 + 2 * q4);
+                // B[k = p][n = i]: a1[p0 + k + t][i0 + gq]; rows past NA1 meet dz2 = 0
+                const int c = i0 + gq;
+                const int r0 = min(p0 + 2 * q4 + t, NA1 - 1), r1 = min(p0 + 2 * q4 + 1 + t, NA1 - 1);
+                const int r2 = min(p0 + 8 + 2 * q4 + t, NA1 - 1), r3 = min(p0 + 9 + 2 * q4 + t, NA1 - 1);
+                const uint32_t b0 = pack2(s.a1[r0 * LDB + c], s.a1[r1 * LDB + c]);
+                const uint32_t b1 = pack2(s.a1[r2 * LDB + c], s.a1[r3 * LDB + c]);
+                mma_bf16(accw[slot], a0, a1, a2, a3, b0, b1);
+            }
+        }
+        // da1[r][i] = sum_{t,o} w2[o][i][t] dz2[r - t][o]: M = r (10 tiles of 16 over NA1), N = i (4), K = (t, o) (10)
+        // then dz1 = da1 * gelu'(z1), db1, dW1
+        for (int m = warp; m < (NA1 + 15) / 16; m += nwarp) {
+            const int r0 = m * 16;
+            float acc[4][4] = {};
+#pragma unroll
+            for (int t = 0; t < KW; ++t) {
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    // A[r][o] = dz2[r - t][o] = dzP[(r - t + 4)][o]; rows beyond the buffer are zero-padded
+                    const int ra = min(r0 + gq - t + 4, NZ2 + 7), rb = min(r0 + gq + 8 - t + 4, NZ2 + 7);
+                    const uint32_t a0 = ld2(&dzP[ra * LDB + 16 * h + 2 * q4]);
+                    const uint32_t a1 = ld2(&dzP[rb * LDB + 16 * h + 2 * q4]);
+                    const uint32_t a2 = ld2(&dzP[ra * LDB + 16 * h + 8 + 2 * q4]);
+                    const uint32_t a3 = ld2(&dzP[rb * LDB + 16 * h + 8 + 2 * q4]);
+#pragma unroll
+                    for (int nt = 0; nt < 4; ++nt) {
+                        // B[k = o][n = i] = w2[o][i][t]: column i contiguous over o is w2[t] transposed;
+                        // w2 smem is [t][o][i], so gather the two o values of the pair
+                        const int ic = nt * 8 + gq;
+                        const int o0 = 16 * h + 2 * q4;
+                        const uint32_t b0 = pack2(s.w2[(t * CH + o0) * LDB + ic], s.w2[(t * CH + o0 + 1) * LDB + ic]);
+                        const uint32_t b1 =
+                            pack2(s.w2[(t * CH + o0 + 8) * LDB + ic], s.w2[(t * CH + o0 + 9) * LDB + ic]);
+                        mma_bf16(acc[nt], a0, a1, a2, a3, b0, b1);
+                    }
+                }
+            }
+#pragma unroll
+            for (int nt = 0; nt < 4; ++nt) {
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    const int r = r0 + gq + (e >= 2 ? 8 : 0), i = nt * 8 + 2 * q4 + (e & 1);
+                    if (r < NA1) s.z1[r * LDF + i] = acc[nt][e] * gelu_grad(s.z1[r * LDF + i]);  // dz1 in place
+                }
+            }
+        }
+        __syncthreads();
+        for (int k = threadIdx.x; k < CH * (KW + 1); k += blockDim.x) {
+            const int o = k / (KW + 1), t = k % (KW + 1);
+            float a = 0.0f;
+            if (t < KW) {
+                for (int r = 0; r < NA1; ++r) a = fmaf(s.z1[r * LDF + o], s.us[r + t], a);
+                g[OW1 + o * KW + t] += a;
+            } else {
+                for (int r = 0; r < NA1; ++r) a += s.z1[r * LDF + o];
+                g[OB1 + o] += a;
+            }
+        }
+        __syncthreads();
+    }
+    // dW2 accumulators -> g (flat w2 is [o][i][t])
+#pragma unroll
+    for (int slot = 0; slot < 5; ++slot) {
+        const int k = warp + slot * 8;
+        const int mo = k / 20, nn = k % 20, t = nn / 4, i0 = (nn % 4) * 8;
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const int o = mo * 16 + gq + (e >= 2 ? 8 : 0), i = i0 + 2 * q4 + (e & 1);
+            g[OW2 + (o * CH + i) * KW + t] += accw[slot][e];
+        }
+    }
+    __syncthreads();
+    float *row = partial + (int64_t)blockIdx.x * (NPARAM + 1);
+    for (int i = threadIdx.x; i < NPARAM + 1; i += blockDim.x) row[i] = g[i];
+}
+
+// Sum the blocks' rows: out[j] = sum_b partial[b][j], j < NPARAM + 1.
+__global__ void k_reduce(const float *__restrict__ partial, int rows, float *__restrict__ out) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= NPARAM + 1) return;
+    float a = 0.0f;
+    for (int b = 0; b < rows; ++b) a += partial[(int64_t)b * (NPARAM + 1) + j];
+    out[j] = a;
+}
+
+// Adam on the FP32 master parameters.
+__global__ void k_adam(float *__restrict__ theta, const float *__restrict__ grad, float *__restrict__ m,
+                       float *__restrict__ v, float lr, float b1, float b2, float eps, float c1, float c2) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= NTRAIN) return;
+    const float gj = grad[j];
+    const float mj = b1 * m[j] + (1.0f - b1) * gj;
+    const float vj = b2 * v[j] + (1.0f - b2) * gj * gj;
+    m[j] = mj;
+    v[j] = vj;
+    theta[j] -= lr * (mj / c1) / (sqrtf(vj / c2) + eps);
+}
+
+// Cell averages of `factor` fine cells: coarse[d][j] = mean(fine[d][factor j .. factor j + factor - 1]).
+__global__ void k_coarse_grain(const double *__restrict__ fine, float *__restrict__ coarse, int64_t n_coarse_total,
+                               int factor) {
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n_coarse_total) return;
+    double a = 0.0;
+    for (int k = 0; k < factor; ++k) a += fine[j * factor + k];
+    coarse[j] = (float)(a / factor);
+}
+
+constexpr size_t smem_bytes() { return sizeof(Smem); }
+
+}  // namespace cl
+}  // namespace sw
+
+using namespace sw;
+
+namespace {
+
+int closure_check(sw_ctx *ctx, int32_t n_dom, int64_t n) {
+    if (!ctx || n_dom < 1 || n < cl::TOUT || n % cl::TOUT) return SW_ERR_SIZE;
+    return SW_OK;
+}
+
+cudaError_t allow_smem() {
+    static bool done = false;
+    if (done) return cudaSuccess;
+    cudaError_t e = cudaFuncSetAttribute(cl::k_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cl::smem_bytes());
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(cl::k_step, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cl::smem_bytes());
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(cl::k_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cl::smem_bytes());
+    done = (e == cudaSuccess);
+    return e;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sw_closure_infer(sw_ctx *ctx, const float *theta, const float *u, float *delta, int32_t n_dom, int64_t n) {
+    int rc = closure_check(ctx, n_dom, n);
+    if (rc) return rc;
+    if (!theta || !u || !delta) return SW_ERR_ARG;
+    SW_CUDA(ctx, cudaSetDevice(ctx->device));
+    SW_CUDA(ctx, allow_smem());
+    const int64_t tiles = n / cl::TOUT;
+    cl::k_infer<<<(unsigned)(tiles * n_dom), cl::THREADS, cl::smem_bytes(), ctx->stream>>>(theta, u, delta, n, tiles);
+    SW_CUDA(ctx, cudaGetLastError());
+    SW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return SW_OK;
+}
+
+int sw_closure_step(sw_ctx *ctx, const sw_config *coarse, const float *theta, float *u, int32_t n_dom, int64_t n,
+                    int64_t n_steps, int32_t use_closure, sw_result *out) {
+    int rc = closure_check(ctx, n_dom, n);
+    if (rc) return rc;
+    if (!coarse || !u || (use_closure && !theta)) return SW_ERR_ARG;
+    if (coarse->problem != SW_KS || coarse->precision != 4) return fail(ctx, SW_ERR_UNSUPPORTED, "closure steps KS FP32");
+    sw_config c = *coarse;
+    c.nx = n;
+    sw_constants k;
+    sw_constants_of(&c, &k);
+    const Params<float> p = make_params<float>(c, k);
+    SW_CUDA(ctx, cudaSetDevice(ctx->device));
+    SW_CUDA(ctx, allow_smem());
+    SW_CUDA(ctx, grow_dev(&ctx->d_work, &ctx->n_work, sizeof(float) * (size_t)n * n_dom));
+    float *alt = static_cast<float *>(ctx->d_work), *cur = u;
+    const int64_t tiles = n / cl::TOUT;
+    SW_CUDA(ctx, cudaEventRecord(ctx->k0, ctx->stream));
+    for (int64_t i = 0; i < n_steps; ++i) {
+        cl::k_step<<<(unsigned)(tiles * n_dom), cl::THREADS, cl::smem_bytes(), ctx->stream>>>(theta, p, cur, alt, n,
+                                                                                                 tiles, use_closure);
+        std::swap(cur, alt);
+    }
+    SW_CUDA(ctx, cudaGetLastError());
+    if (cur != u) SW_CUDA(ctx, cudaMemcpyAsync(u, cur, sizeof(float) * (size_t)n * n_dom, cudaMemcpyDeviceToDevice,
+                                               ctx->stream));
+    SW_CUDA(ctx, cudaEventRecord(ctx->k1, ctx->stream));
+    SW_CUDA(ctx, cudaEventSynchronize(ctx->k1));
+    if (out) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, ctx->k0, ctx->k1);
+        std::memset(out, 0, sizeof(*out));
+        out->n_steps = n_steps;
+        out->t_final = n_steps * c.dt;
+        out->kernel_ms = out->elapsed_ms = ms;
+        out->launches = n_steps;
+    }
+    return SW_OK;
+}
+
+int sw_closure_grad(sw_ctx *ctx, const float *theta, const float *u, const float *target, const int64_t *rows,
+                    int32_t n_dom, int64_t n, float *grad_and_loss) {
+    int rc = closure_check(ctx, n_dom, n);
+    if (rc) return rc;
+    if (!theta || !u || !target || !grad_and_loss) return SW_ERR_ARG;
+    SW_CUDA(ctx, cudaSetDevice(ctx->device));
+    SW_CUDA(ctx, allow_smem());
+    const int64_t tiles_per = n / cl::TOUT, n_tiles = tiles_per * n_dom;
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    const int64_t grid = std::min<int64_t>(n_tiles, (int64_t)sms * 2);
+    SW_CUDA(ctx, grow_dev(&ctx->d_io, &ctx->n_io, sizeof(float) * (size_t)grid * (cl::NPARAM + 1)));
+    float *partial = static_cast<float *>(ctx->d_io);
+    const float scale = 1.0f / (float)((double)n_dom * n);
+    cl::k_grad<<<(unsigned)grid, cl::THREADS, cl::smem_bytes(), ctx->stream>>>(theta, u, target, rows, partial, n,
+                                                                                tiles_per, n_tiles, scale);
+    SW_CUDA(ctx, cudaGetLastError());
+    cl::k_reduce<<<(cl::NPARAM + 1 + 255) / 256, 256, 0, ctx->stream>>>(partial, (int)grid, grad_and_loss);
+    SW_CUDA(ctx, cudaGetLastError());
+    SW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return SW_OK;
+}
+
+int sw_closure_adam(sw_ctx *ctx, float *theta, const float *grad, float *m, float *v, int32_t step, float lr) {
+    if (!ctx || !theta || !grad || !m || !v || step < 1) return SW_ERR_ARG;
+    const float b1 = 0.9f, b2 = 0.999f;
+    const float c1 = 1.0f - std::pow(b1, (float)step), c2 = 1.0f - std::pow(b2, (float)step);
+    cl::k_adam<<<(cl::NTRAIN + 255) / 256, 256, 0, ctx->stream>>>(theta, grad, m, v, lr, b1, b2, 1e-8f, c1, c2);
+    SW_CUDA(ctx, cudaGetLastError());
+    return SW_OK;
+}
+
+int sw_closure_train(sw_ctx *ctx, float *theta, const float *inputs, const float *targets, int64_t n_samples,
+                     int64_t n, int32_t batch, int32_t steps, float lr, uint64_t seed, float *loss_host) {
+    int rc = closure_check(ctx, batch, n);
+    if (rc) return rc;
+    if (!theta || !inputs || !targets || n_samples < 1 || steps < 0) return SW_ERR_ARG;
+    SW_CUDA(ctx, cudaSetDevice(ctx->device));
+    // Adam moments and a gradient row live in one allocation owned by this call
+    float *buf = nullptr;
+    int64_t *rows = nullptr;
+    SW_CUDA(ctx, cudaMalloc(&buf, sizeof(float) * (3 * cl::NPARAM + 2)));
+    cudaError_t e = cudaMalloc(&rows, sizeof(int64_t) * (size_t)batch);
+    if (e != cudaSuccess) {
+        cudaFree(buf);
+        return cuda_fail(ctx, e, "cudaMalloc rows");
+    }
+    float *m = buf, *v = buf + cl::NPARAM, *grad = buf + 2 * cl::NPARAM;
+    cudaMemsetAsync(buf, 0, sizeof(float) * 2 * cl::NPARAM, ctx->stream);
+    std::vector<int64_t> host_rows((size_t)batch);
+    uint64_t st = seed ? seed : 0x9E3779B97F4A7C15ull;
+    for (int32_t s = 0; s < steps && rc == SW_OK; ++s) {
+        for (auto &r : host_rows) {  // splitmix64 draws of the minibatch rows
+            st += 0x9E3779B97F4A7C15ull;
+            uint64_t z = st;
+            z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+            z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+            r = (int64_t)((z ^ (z >> 31)) % (uint64_t)n_samples);
+        }
+        e = cudaMemcpyAsync(rows, host_rows.data(), sizeof(int64_t) * batch, cudaMemcpyHostToDevice, ctx->stream);
+        if (e != cudaSuccess) { rc = cuda_fail(ctx, e, "rows"); break; }
+        rc = sw_closure_grad(ctx, theta, inputs, targets, rows, batch, n, grad);
+        if (rc) break;
+        if (loss_host) {
+            e = cudaMemcpy(&loss_host[s], grad + cl::NPARAM, sizeof(float), cudaMemcpyDeviceToHost);
+            if (e != cudaSuccess) { rc = cuda_fail(ctx, e, "loss"); break; }
+        }
+        rc = sw_closure_adam(ctx, theta, grad, m, v, s + 1, lr);
+    }
+    cudaStreamSynchronize(ctx->stream);
+    cudaFree(rows);
+    cudaFree(buf);
+    return rc;
+}
+
+int sw_coarse_grain(sw_ctx *ctx, const double *fine, float *coarse, int64_t n_coarse_total, int32_t factor) {
+    if (!ctx || !fine || !coarse || n_coarse_total < 1 || factor < 1) return SW_ERR_ARG;
+    SW_CUDA(ctx, cudaSetDevice(ctx->device));
+    cl::k_coarse_grain<<<(unsigned)((n_coarse_total + 255) / 256), 256, 0, ctx->stream>>>(fine, coarse,
+                                                                                            n_coarse_total, factor);
+    SW_CUDA(ctx, cudaGetLastError());
+    SW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return SW_OK;
+}
+
+}  // extern "C"

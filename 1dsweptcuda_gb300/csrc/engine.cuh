@@ -28,6 +28,7 @@
 
 #include <cuda_runtime.h>
 
+#include <climits>
 #include <cstdint>
 #include <type_traits>
 
@@ -76,10 +77,28 @@ __device__ __forceinline__ typename Scheme<P, T>::G tile_get(const T *rows, int 
     }
 }
 
+// Tile coordinates of the domain's first and last cell (global 0 and nx-1),
+// or a sentinel outside [-R, W+R) when the tile does not hold them.  Boundary
+// conditions then cost two integer compares per cell instead of a wrapped
+// 64-bit position.
+struct Ends {
+    int first, last;
+};
+__device__ __forceinline__ int tile_coord_of(int64_t g, int64_t base, int64_t nx, int lo, int hi) {
+    int64_t x = (g - base) % nx;
+    if (x < 0) x += nx;
+    if (x < hi) return (int)x;
+    if (x - nx >= lo) return (int)(x - nx);
+    return INT32_MIN / 2;
+}
+__device__ __forceinline__ Ends tile_ends(int64_t base, int64_t nx, int W, int R) {
+    return Ends{tile_coord_of(0, base, nx, -R, W + R), tile_coord_of(nx - 1, base, nx, -R, W + R)};
+}
+
 // One sub-step of parity `par` (1: predictor / odd Heat step; 0: corrector /
-// even Heat step) at tile cell x, global position gp.
+// even Heat step) at tile cell x.
 template <int P, typename T>
-__device__ __forceinline__ void tile_point(const Params<T> &p, T *rows, int L, int par, int x, int64_t gp) {
+__device__ __forceinline__ void tile_point(const Params<T> &p, T *rows, int L, int par, int x, Ends e) {
     constexpr int R = Scheme<P, T>::R;
     constexpr int C = Scheme<P, T>::C;
     const T *src = rows + (par ^ 1) * C * L + R;
@@ -87,8 +106,8 @@ __device__ __forceinline__ void tile_point(const Params<T> &p, T *rows, int L, i
     if constexpr (P == SW_HEAT) {
         int l = x - 1, r = x + 1;
         if (p.bc != SW_BC_PERIODIC) {  // insulated ends, Heat1D_SweptShared.cu:140-142,352-353
-            if (gp == 0) l = x + 1;
-            if (gp == p.nx - 1) r = x - 1;
+            if (x == e.first) l = x + 1;
+            if (x == e.last) r = x - 1;
         }
         dst[x] = heat_step(p, src[l], src[x], src[r]);
     } else if constexpr (P == SW_KS) {
@@ -97,8 +116,8 @@ __device__ __forceinline__ void tile_point(const Params<T> &p, T *rows, int L, i
         else
             dst[x] = ks_correct(p, dst[x], src[x - 2], src[x - 1], src[x], src[x + 1], src[x + 2]);
     } else {
-        if (gp == 0 || gp == p.nx - 1) return;  // Dirichlet cells, Euler1D_SweptShared.cu:405-416
-        const bool fl = (gp == 1), fr = (gp == p.nx - 2);
+        if (x == e.first || x == e.last) return;  // Dirichlet cells, Euler1D_SweptShared.cu:405-416
+        const bool fl = (x == e.first + 1), fr = (x == e.last - 1);
         Q3<T> s[5];
 #pragma unroll
         for (int k = 0; k < 5; ++k) s[k] = q3(src[x - 2 + k], src[L + x - 2 + k], src[2 * L + x - 2 + k]);
@@ -183,9 +202,10 @@ template <int P, typename T>
 __device__ __forceinline__ void tile_down(const Params<T> &p, T *rows, int L, int W, int64_t base) {
     constexpr int R = Scheme<P, T>::R;
     const int h = W >> 1, H = W / (2 * R);
+    const Ends e = tile_ends(base, p.nx, W, R);
     for (int j = 1; j <= H; ++j) {
         for (int x = threadIdx.x; x < W; x += blockDim.x)
-            if (x >= h - j * R && x < h + j * R) tile_point<P, T>(p, rows, L, j & 1, x, wrap_pos(base + x, p.nx));
+            if (x >= h - j * R && x < h + j * R) tile_point<P, T>(p, rows, L, j & 1, x, e);
         __syncthreads();
     }
 }
@@ -194,9 +214,10 @@ template <int P, typename T>
 __device__ __forceinline__ void tile_up(const Params<T> &p, T *rows, int L, int W, int64_t base) {
     constexpr int R = Scheme<P, T>::R;
     const int H = W / (2 * R);
+    const Ends e = tile_ends(base, p.nx, W, R);
     for (int u = 1; u < H; ++u) {
         for (int x = threadIdx.x; x < W; x += blockDim.x)
-            if (x >= u * R && x < W - u * R) tile_point<P, T>(p, rows, L, u & 1, x, wrap_pos(base + x, p.nx));
+            if (x >= u * R && x < W - u * R) tile_point<P, T>(p, rows, L, u & 1, x, e);
         __syncthreads();
     }
 }

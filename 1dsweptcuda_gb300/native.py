@@ -28,7 +28,9 @@ ERRORS = {0: "SW_OK", -1: "SW_ERR_ARG", -2: "SW_ERR_SIZE", -3: "SW_ERR_UNSTABLE"
 EXPORTED = ["sw_abi_version", "sw_strerror", "sw_ctx_create", "sw_ctx_destroy", "sw_ctx_last_error",
             "sw_config_init", "sw_validate", "sw_constants_of", "sw_initial_condition", "sw_run",
             "sw_run_device", "sw_plan", "sw_cli_main", "sw_run_batch", "sw_run_batch_device",
-            "sw_query_tuning", "sw_run_device_noalloc"]
+            "sw_query_tuning", "sw_run_device_noalloc", "sw_closure_infer", "sw_closure_step",
+            "sw_closure_grad", "sw_closure_adam", "sw_closure_train", "sw_coarse_grain"]
+CLOSURE_PARAMS = 5506
 NOALLOC_SCRATCH_BYTES = 24 * 1024 * 1024
 
 
@@ -123,9 +125,18 @@ def library():
     L.sw_run_batch_device.argtypes = [C.c_void_p, cp, C.c_int32, i64p, C.c_void_p, C.c_void_p, rp]
     L.sw_query_tuning.argtypes = [C.c_void_p, cp, C.c_int32, i64p, C.POINTER(Tuning)]
     L.sw_run_device_noalloc.argtypes = [cp, C.c_void_p, C.c_void_p]
+    vp = C.c_void_p
+    L.sw_closure_infer.argtypes = [vp, vp, vp, vp, C.c_int32, C.c_int64]
+    L.sw_closure_step.argtypes = [vp, cp, vp, vp, C.c_int32, C.c_int64, C.c_int64, C.c_int32, rp]
+    L.sw_closure_grad.argtypes = [vp, vp, vp, vp, vp, C.c_int32, C.c_int64, vp]
+    L.sw_closure_adam.argtypes = [vp, vp, vp, vp, vp, C.c_int32, C.c_float]
+    L.sw_closure_train.argtypes = [vp, vp, vp, vp, C.c_int64, C.c_int64, C.c_int32, C.c_int32, C.c_float,
+                                   C.c_uint64, C.POINTER(C.c_float)]
+    L.sw_coarse_grain.argtypes = [vp, vp, vp, C.c_int64, C.c_int32]
     for name in ("sw_ctx_create", "sw_ctx_destroy", "sw_config_init", "sw_validate", "sw_constants_of",
                  "sw_initial_condition", "sw_run", "sw_run_device", "sw_cli_main", "sw_plan", "sw_run_batch",
-                 "sw_run_batch_device", "sw_query_tuning", "sw_run_device_noalloc"):
+                 "sw_run_batch_device", "sw_query_tuning", "sw_run_device_noalloc", "sw_closure_infer",
+                 "sw_closure_step", "sw_closure_grad", "sw_closure_adam", "sw_closure_train", "sw_coarse_grain"):
         getattr(L, name).restype = C.c_int
     _lib = L
     return L

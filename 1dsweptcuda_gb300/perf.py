@@ -38,12 +38,49 @@ def cases(quick: bool):
     return c
 
 
+def ensemble_rows(sw, solver, quick: bool):
+    """Config 4 shape: 4096 periodic KS domains, nx log-uniform in 2^10..2^16 (seeded),
+    dx = 0.5, dt = 0.005; swept (autotuned tile), variant and classic, FP32 and FP64,
+    over a window of time steps (FP32: the full tf = 100, 20000 steps)."""
+    import numpy as np
+    import torch
+    ens = __import__("importlib").import_module("1dsweptcuda_gb300.ensemble")
+    nx, u = ens.make_ensemble(n_domains=256 if quick else 4096)
+    rows = []
+    for prec, steps in ((4, 1024 if quick else 20000), (8, 512 if quick else 2048)):
+        dt = np.float64 if prec == 8 else np.float32
+        ic = u.astype(dt)
+        tuned = None
+        out = {}
+        for alg in (sw.ALG_SWEPT, sw.ALG_VARIANT, sw.ALG_CLASSIC):
+            n = steps if alg != sw.ALG_CLASSIC else min(steps, 512)
+            cfg = sw.make_config(sw.KS, prec, alg=alg, tpb=0 if alg != sw.ALG_CLASSIC else 256, dt=0.005,
+                                 time_mode=sw.TIME_STEPS, n_steps=n)
+            if alg == sw.ALG_SWEPT:
+                tuned = solver.tune(cfg, nx)
+            st = torch.from_numpy(ic.copy()).cuda()
+            res = solver.run_batch_device(cfg, nx, st.data_ptr())
+            ups = float(nx.sum()) * n / (res.kernel_ms * 1e-3)
+            out[alg] = (st.cpu().numpy(), n)
+            rows.append({"case": "ks ensemble 4096 domains" if not quick else "ks ensemble 256 domains",
+                         "precision": prec, "alg": {1: "swept", 2: "variant", 0: "classic"}[alg],
+                         "tile": res.tile, "threads": tuned.threads if tuned and alg else None,
+                         "cells": int(nx.sum()), "steps": n, "ms": res.kernel_ms, "cell_updates_per_s": ups,
+                         "launches": res.launches})
+            print("%-34s f%-2d %-8s tile=%-5s %10.3e cell-updates/s (%d steps, %.1f ms)" % (
+                rows[-1]["case"], prec * 8, rows[-1]["alg"], res.tile, ups, n, res.kernel_ms), flush=True)
+        rows[-3]["equal_to_variant"] = bool(np.array_equal(out[1][0], out[2][0]))
+        rows[-3]["tuning"] = tuned.candidates()
+    return rows
+
+
 def main():
     import numpy as np
     import torch
 
     ap = argparse.ArgumentParser()
     ap.add_argument("--quick", action="store_true")
+    ap.add_argument("--ensemble", action="store_true", help="also run the ensemble (config 4) rows")
     ap.add_argument("--json", default=None)
     args = ap.parse_args()
     sw = importlib.import_module("1dsweptcuda_gb300")
@@ -94,6 +131,8 @@ def main():
                 print("%-34s f%-2d %-8s tpb=%-5s %10.3e cell-updates/s  x%.2f vs classic  %s" % (
                     label, prec * 8, r["alg"], r["tpb"], r["cell_updates_per_s"], r.get("over_classic", 1.0),
                     "bit-identical" if r.get("equal_to_classic") else "DIFFERS"), flush=True)
+    if args.ensemble:
+        rows += ensemble_rows(sw, solver, args.quick)
     solver.close()
     if args.json:
         Path(args.json).write_text(json.dumps(rows, indent=1))

@@ -206,6 +206,44 @@ int sw_run_batch_device(sw_ctx *ctx, const sw_config *cfg, int32_t n_domains, co
  * The choice is remembered by the context for this ensemble shape. */
 int sw_query_tuning(sw_ctx *ctx, const sw_config *cfg, int32_t n_domains, const int64_t *nx, sw_tuning *out);
 
+/* ------------------------------------------------------------ KS closure
+ * No counterpart in the reference (the learned extension): a 3-layer 1D
+ * convolution, 1 -> 32 -> 32 -> 1 channels, kernel 5, GELU, circular padding
+ * per domain, that corrects a 4x-coarsened KS step:
+ *     u(t + dt) = coarse KS step(u(t)) + f(u(t)).
+ * Parameters are SW_CLOSURE_PARAMS FP32 values laid out
+ *     w1[32][5] b1[32] | w2[32][32][5] b2[32] | w3[32][5] b3[1] | s[1]
+ * (w[out][in][tap], tap t multiplies u[x + t - 2]); f(u) = s * net(u), the
+ * output scale s is chosen by the caller (e.g. the spread of the training
+ * targets) and never trained.  Weights are rounded to BF16 for the forward
+ * pass; the 32 -> 32 layer runs on the tensor cores (BF16 x BF16,
+ * FP32 accumulation), forward and backward.  Every array argument is a
+ * device pointer; states are float32 domains of n cells (n a multiple of
+ * 128) stored one after another.  The calls run on the context's stream and
+ * return when done. */
+#define SW_CLOSURE_PARAMS 5506
+/* delta = f(u) for n_dom domains. */
+int sw_closure_infer(sw_ctx *ctx, const float *theta, const float *u, float *delta, int32_t n_dom, int64_t n);
+/* n_steps coarse KS steps (coarse: problem SW_KS, precision 4, its dt and dx)
+ * fused with the closure (use_closure = 0: the plain coarse step), in place. */
+int sw_closure_step(sw_ctx *ctx, const sw_config *coarse, const float *theta, float *u, int32_t n_dom, int64_t n,
+                    int64_t n_steps, int32_t use_closure, sw_result *out);
+/* Loss L = mean over points of (net(u) - target / s)^2 over the n_dom domains
+ * (rows[d] selects the sample for domain d when rows is non-NULL) and its
+ * gradient: grad_and_loss[0..SW_CLOSURE_PARAMS-1] = dL/dtheta (0 for s),
+ * [SW_CLOSURE_PARAMS] = L. */
+int sw_closure_grad(sw_ctx *ctx, const float *theta, const float *u, const float *target, const int64_t *rows,
+                    int32_t n_dom, int64_t n, float *grad_and_loss);
+/* One Adam step (beta1 0.9, beta2 0.999, eps 1e-8) on the FP32 parameters; m, v zero at step 1. */
+int sw_closure_adam(sw_ctx *ctx, float *theta, const float *grad, float *m, float *v, int32_t step, float lr);
+/* `steps` Adam steps on minibatches of `batch` samples drawn (seeded) from
+ * n_samples (input, target) pairs of n cells; loss_host (optional, host,
+ * `steps` floats) receives the loss of each step. */
+int sw_closure_train(sw_ctx *ctx, float *theta, const float *inputs, const float *targets, int64_t n_samples,
+                     int64_t n, int32_t batch, int32_t steps, float lr, uint64_t seed, float *loss_host);
+/* Cell averages of `factor` consecutive fine FP64 cells into FP32 coarse cells. */
+int sw_coarse_grain(sw_ctx *ctx, const double *fine, float *coarse, int64_t n_coarse_total, int32_t factor);
+
 /* ------------------------------------------------ no-allocation entry point
  * No counterpart in the reference.  For callers that cannot allocate device
  * memory when they step the solver: codes that size all GPU memory once at

@@ -9,9 +9,11 @@ in FP32 with the BF16-rounded weights.  This module restates that arithmetic
 in float64 (with the same BF16 rounding points) and its gradients, so the GPU
 kernels' forward outputs and weight gradients can be checked against it.
 
-Parameter layout (flat FP32 vector, PARAMS = 5505 values):
-  w1[32][5] b1[32] | w2[32][32][5] b2[32] | w3[32][5] b3[1]
-  w[out][in][tap], tap t multiplies u[x + t - 2].
+Parameter layout (flat FP32 vector, PARAMS = 5506 values):
+  w1[32][5] b1[32] | w2[32][32][5] b2[32] | w3[32][5] b3[1] | s[1]
+  w[out][in][tap], tap t multiplies u[x + t - 2]; delta = s * net(u), the
+  output scale s is fixed (not trained).  The loss is on the scaled defect:
+  mean (net(u) - target / s)^2.
 """
 from __future__ import annotations
 
@@ -21,7 +23,8 @@ import numpy as np
 
 C = 32
 K = 5
-SIZES = [("w1", (C, K)), ("b1", (C,)), ("w2", (C, C, K)), ("b2", (C,)), ("w3", (C, K)), ("b3", (1,))]
+SIZES = [("w1", (C, K)), ("b1", (C,)), ("w2", (C, C, K)), ("b2", (C,)), ("w3", (C, K)), ("b3", (1,)),
+         ("scale", (1,))]
 PARAMS = sum(int(np.prod(s)) for _, s in SIZES)
 
 
@@ -61,6 +64,7 @@ def init(seed: int = 0, scale: float = 1.0) -> np.ndarray:
         "b2": np.zeros(C),
         "w3": rng.standard_normal((C, K)) * 1e-3,
         "b3": np.zeros(1),
+        "scale": np.ones(1),
     }
     return pack(d).astype(np.float32)
 
@@ -96,19 +100,21 @@ def forward(theta: np.ndarray, u: np.ndarray, keep: bool = False):
     z2 = np.einsum("oit,bitn->bon", w2, t1) + p["b2"][None, :, None]
     a2 = gelu(z2)
     t2 = _taps(a2)                                       # (b, C, K, n)
-    delta = np.einsum("it,bitn->bn", w3, t2) + p["b3"][0]
+    raw = np.einsum("it,bitn->bn", w3, t2) + p["b3"][0]
     if keep:
-        return delta, dict(u=u, tu=tu, z1=z1, a1q=a1q, t1=t1, z2=z2, a2=a2, t2=t2)
-    return delta
+        return raw, dict(u=u, tu=tu, z1=z1, a1q=a1q, t1=t1, z2=z2, a2=a2, t2=t2)
+    return np.float32(p["scale"][0]) * raw
 
 
 def loss_and_grad(theta: np.ndarray, u: np.ndarray, target: np.ndarray):
-    """Mean squared error over all points and its gradient with respect to the
-    FP32 parameters (straight-through for the BF16 roundings)."""
-    delta, s = forward(theta, u, keep=True)
-    target = np.asarray(target, dtype=np.float64).reshape(delta.shape)
-    npts = delta.size
-    err = delta - target
+    """Mean squared scaled defect, mean (net(u) - target/s)^2, and its gradient
+    with respect to the FP32 parameters (straight-through for the BF16
+    roundings; zero for the fixed scale s)."""
+    raw, s = forward(theta, u, keep=True)
+    target = np.asarray(target, dtype=np.float64).reshape(raw.shape)
+    scl = float(np.float32(unpack(theta)["scale"][0]))
+    npts = raw.size
+    err = raw - np.asarray(np.asarray(target, dtype=np.float32) / np.float32(scl), dtype=np.float64)
     loss = float(np.sum(err * err) / npts)
     g = 2.0 * err / npts                                  # dL/ddelta (b, n)
     p = unpack(theta)
@@ -127,6 +133,7 @@ def loss_and_grad(theta: np.ndarray, u: np.ndarray, target: np.ndarray):
     dz1 = da1 * gelu_grad(s["z1"])
     grads["b1"] = dz1.sum(axis=(0, 2))
     grads["w1"] = np.einsum("bon,btn->ot", dz1, s["tu"])
+    grads["scale"] = np.zeros(1)
     return loss, pack(grads)
 
 

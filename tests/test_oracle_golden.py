@@ -154,3 +154,37 @@ def test_fp32_close_to_fp64(oracle, problem):
     u32 = oracle.classic(oracle.reference_consts(problem, 4, nx, dt), oracle.reference_ic(problem, 4, nx), 50)
     scale = np.abs(u64).max()
     assert np.abs(u32.astype(np.float64) - u64).max() / scale < 1e-5
+
+
+def test_closure_oracle_gradient_is_exact():
+    """The closure oracle's analytic gradient equals central differences of its
+    loss (BF16 rounding switched off, since it makes the loss piecewise constant)."""
+    from oracle import closure as ocl
+    th = ocl.init(1).astype(np.float64)
+    rng = np.random.default_rng(3)
+    th[5344:5505] = rng.standard_normal(161) * 0.1
+    th[5505] = 0.7
+    u = rng.standard_normal((2, 64))
+    tgt = rng.standard_normal((2, 64)) * 0.1
+    saved = ocl.bf16
+    ocl.bf16 = lambda x: np.asarray(x, dtype=np.float64)
+    try:
+        _, g = ocl.loss_and_grad(th, u, tgt)
+        assert g[5505] == 0.0
+        for i in (0, 40, 100, 170, 200, 3000, 5300, 5320, 5400, 5504):
+            e = np.zeros_like(th)
+            e[i] = 1e-6
+            fd = (ocl.loss_and_grad(th + e, u, tgt)[0] - ocl.loss_and_grad(th - e, u, tgt)[0]) / 2e-6
+            assert abs(g[i] - fd) <= 1e-6 * max(1.0, abs(fd)), (i, g[i], fd)
+    finally:
+        ocl.bf16 = saved
+
+
+def test_closure_oracle_bf16_rounding():
+    from oracle import closure as ocl
+    x = np.array([1.0, 1.00390625, 1.005859375, 3.14159, -2.5e-3, 0.0], dtype=np.float32)
+    r = ocl.bf16(x)
+    assert r[0] == 1.0 and r[1] == 1.0      # halfway: ties to even
+    assert r[2] == 1.0078125                # above halfway rounds up
+    assert abs(r[3] - 3.140625) < 1e-12
+    assert (ocl.bf16(r) == r).all()          # idempotent
