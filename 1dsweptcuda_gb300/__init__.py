@@ -14,7 +14,7 @@ from .native import (  # noqa: F401
     EULER, HEAT, KS, TIME_REFERENCE, TIME_STEPS, Config, Constants, NativeError, Result, Solver, cli_main,
     constants, initial_condition, library, library_path, make_config, plan, validate,
 )
-from .formats import Perform, Solved, read_dat, write_timing_header  # noqa: F401
+from .formats import Perform, Solved, read_dat, read_snapshots, write_timing_header  # noqa: F401
 from .runner import runCUDA, binary_path  # noqa: F401
 
 __all__ = [

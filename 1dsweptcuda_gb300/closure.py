@@ -9,9 +9,11 @@ FP32.  The closure f learns the coarse step's defect
 CG = averages of 4 fine cells, so that u(t + dt) = coarse(u) + f(u) tracks the
 coarse-grained fine solution.  Training data come from the project's own fine
 ensemble solver; training runs on the GPU through sw_closure_train (forward and
-backward on BF16 tensor cores, Adam on FP32 masters).  A run with the closure
-falls back to the fine solver for domains whose residual estimate -- the size of
-the correction relative to the coarse update -- exceeds a threshold.
+backward on BF16 tensor cores, Adam on FP32 masters).  run_adaptive checks each
+segment against one prolonged fine step (a residual of the coarse update with
+respect to the fine dynamics), picks the closure-corrected or the plain coarse
+update per domain, accumulates the residuals into a per-domain error estimate,
+and hands the domains whose estimate passes a tolerance to the fine solver.
 """
 from __future__ import annotations
 
@@ -183,125 +185,177 @@ def rel_l2(a, b) -> float:
 
 
 def prolong(coarse, factor: int = FACTOR):
-    """Coarse FP32 -> fine FP64 by periodic linear interpolation of cell averages
-    (the fallback's restart state)."""
+    """Coarse cell averages (n_dom, n) -> fine cell averages (n_dom, n * factor),
+    FP64, by periodic spectral interpolation.  Each Fourier mode below the
+    coarse Nyquist frequency is taken from coarse-cell to fine-cell averages
+    (times sinc(k/(n*factor)) / sinc(k/n), with the phase of the shifted cell
+    centres); the Nyquist mode b(-1)^j becomes the fine averages of
+    b*(pi/2)*sin(pi*x/H), H the coarse cell.  Averaging each `factor` fine
+    cells gives the coarse state back (to FP64 rounding), and a band-limited
+    field is reproduced exactly -- the fallback's and the residual check's
+    restart state."""
     torch = _torch()
     c = coarse.double()
-    nxt = torch.roll(c, -1, dims=1)
-    w = (torch.arange(factor, dtype=torch.float64, device=c.device) + 0.5) / factor - 0.5
-    lo = torch.where(w < 0, torch.roll(c, 1, dims=1)[..., None], c[..., None])
-    hi = torch.where(w < 0, c[..., None], nxt[..., None])
-    a = torch.where(w < 0, w + 1.0, w)
-    return (lo * (1 - a) + hi * a).reshape(c.shape[0], -1).contiguous()
+    n_dom, n = c.shape
+    nf = n * factor
+    dev = c.device
+    j = torch.arange(n, device=dev)
+    sign = 1.0 - 2.0 * (j % 2).double()
+    b = (c * sign).mean(dim=1, keepdim=True)
+    spec = torch.fft.rfft(c - b * sign, dim=1)
+    k = torch.arange(n // 2, device=dev, dtype=torch.float64)
+    ratio = torch.sinc(k / nf) / torch.sinc(k / n)
+    phase = torch.exp(1j * math.pi * k / n * (1.0 / factor - 1.0))
+    fine_spec = torch.zeros((n_dom, nf // 2 + 1), dtype=spec.dtype, device=dev)
+    fine_spec[:, :n // 2] = spec[:, :n // 2] * (factor * ratio * phase)
+    fine = torch.fft.irfft(fine_spec, n=nf, dim=1)
+    m = torch.arange(nf, device=dev, dtype=torch.float64)
+    nyq = 0.5 * factor * (torch.cos(math.pi * m / factor) - torch.cos(math.pi * (m + 1) / factor))
+    return (fine + b * nyq).contiguous()
 
 
-def run_with_fallback(solver, closure: Closure, u, coarse_steps: int, segment: int, tau: float):
-    """Closure-corrected coarse run with the fine solver as fallback.  After each
-    segment, domains whose residual estimate ||f(u)|| / ||coarse(u) - u|| (the
-    relative size of the learned correction, i.e. how far the coarse step is
-    from the fine one) exceeds tau are re-run over that segment on the fine grid
-    from the prolonged segment-start state and restricted back.  Returns the
-    number of (domain, segment) fallbacks."""
+def run_adaptive(solver, closure: Closure, fine0, coarse_steps: int, segment: int, tau: float):
+    """Closure-corrected coarse run of an ensemble with a residual-based error
+    estimate and the plain fine solver as fallback.
+
+    fine0: (n_dom, 4096) FP64 states at t0 (the problem as posed).  The coarse
+    state starts at CG(fine0).  At the start of each segment of `segment`
+    coarse steps, every live domain's state u is prolonged (conservatively) to
+    the fine grid and advanced by one coarse step of the fine solver; r, its
+    coarse-grained result, is what one coarse update should reach.  The
+    residuals d_c = ||coarse(u) + f(u) - r||, d_p = ||coarse(u) - r|| pick the
+    closure-corrected or the plain coarse update for the segment, and the
+    smaller one, times the segment's steps over ||u||, is added to the
+    domain's error estimate (a relative L2 error, accumulated without growth).
+    A domain leaves the coarse run as soon as its estimate, projected to the
+    end at the current residual, passes tau; at the end all such domains are
+    solved by the fine solver from fine0, in one batch, so their results are
+    the fine solution itself.
+
+    Returns (u, info): u (n_dom, 1024) FP32 at t0 + coarse_steps * 0.02, and
+    counts of (domain, segment) pairs run with the closure / plain, the
+    domains that fell back, and each domain's final estimate."""
     torch = _torch()
-    fallbacks = 0
+    u = coarse_grain(solver, fine0)
+    n_dom = u.shape[0]
+    live = torch.ones(n_dom, dtype=torch.bool, device=u.device)
+    est = torch.zeros(n_dom, dtype=torch.float64, device=u.device)
+    info = {"closure": 0, "plain": 0, "fallback": 0}
     done = 0
     while done < coarse_steps:
+        idx = torch.nonzero(live).flatten()
+        if idx.numel() == 0:
+            break
         k = min(segment, coarse_steps - done)
-        start = u.clone()
-        plain = start.clone()
-        closure.step(plain, 1, use_closure=False)
-        est = closure.infer(start).norm(dim=1) / (plain - start).norm(dim=1).clamp_min(1e-30)
-        closure.step(u, k, use_closure=True)
-        bad = torch.nonzero(est > tau).flatten()
-        if bad.numel():
-            fallbacks += int(bad.numel())
-            f = prolong(start[bad])
-            advance_fine(solver, f, k * FACTOR)
-            u[bad] = coarse_grain(solver, f)
+        start = u[idx].contiguous()
+        one_c, one_p = start.clone(), start.clone()
+        closure.step(one_c, 1, use_closure=True)
+        closure.step(one_p, 1, use_closure=False)
+        chk = prolong(start)
+        advance_fine(solver, chk, FACTOR)
+        r = coarse_grain(solver, chk)
+        d_c = (one_c - r).double().norm(dim=1)
+        d_p = (one_p - r).double().norm(dim=1)
+        use_c = d_c <= d_p
+        rate = torch.minimum(d_c, d_p) / start.double().norm(dim=1).clamp_min(1e-30)
+        est[idx] += k * rate
+        bad = est[idx] + (coarse_steps - done - k) * rate > tau
+        live[idx[bad]] = False
+        for mask, on in ((use_c & ~bad, True), (~use_c & ~bad, False)):
+            sel = idx[mask]
+            if sel.numel():
+                v = start[mask].contiguous()
+                closure.step(v, k, use_closure=on)
+                u[sel] = v
+                info["closure" if on else "plain"] += int(sel.numel())
         done += k
-    return fallbacks
+    fb = torch.nonzero(~live).flatten()
+    if fb.numel():
+        f = fine0[fb].contiguous().clone()
+        advance_fine(solver, f, coarse_steps * FACTOR)
+        u[fb] = coarse_grain(solver, f)
+    info["fallback"] = int(fb.numel())
+    info["estimate"] = est
+    return u, info
 
 
 CHAOS_SPINUP = 12500   # coarse steps (t = 250): the ensemble's long waves have broken into KS chaos
 
 
-def evaluate(n_train: int = 512, snapshots: int = 64, n_eval: int = 1024, tf: float = 200.0, train_steps: int = 3000,
-             seed: int = 0, tau: float = float("inf"), segment: int = 50, start_step: int = CHAOS_SPINUP) -> dict:
-    """Train on the fine solver's trajectories (developed chaos, t >= 250), then
-    run the evaluation ensemble (n_eval domains, config 5 shape) from
-    t0 = start_step * 0.02 for tf three ways -- fine FP64 (the judge), plain
-    coarse, closure-corrected coarse (with fallback when tau is finite) -- and
-    report times and the relative L2 error against the coarse-grained judge."""
+def _timed(fn):
     import time
+    torch = _torch()
+    torch.cuda.synchronize()
+    a = time.perf_counter()
+    out = fn()
+    torch.cuda.synchronize()
+    return out, time.perf_counter() - a
+
+
+def train_closure(solver, n_train: int = 512, snapshots: int = 64, train_steps: int = 3000, seed: int = 0):
+    """A closure trained on the fine solver's own trajectories in developed
+    chaos (t >= 250), and a summary of the training."""
+    torch = _torch()
+    closure = Closure(solver, seed=seed)
+    info = {"n_train_traj": n_train, "snapshots": snapshots}
+    (x, y), info["datagen_s"] = _timed(lambda: make_training_data(solver, closure, n_train, snapshots, interval=25,
+                                                                  seed=seed + 1, spinup=CHAOS_SPINUP))
+    info["output_scale"] = closure.calibrate(y)
+    losses, info["train_s"] = _timed(lambda: closure.train(x, y, steps=train_steps, batch=64, lr=2e-3,
+                                                           seed=seed + 2))
+    info["loss_first"], info["loss_last"] = float(losses[:10].mean()), float(losses[-50:].mean())
+    hx, hy = make_training_data(solver, closure, 32, 8, interval=25, seed=seed + 999, spinup=CHAOS_SPINUP)
+    info["heldout_defect_ratio"] = float(((hy - closure.infer(hx)).pow(2).sum() / hy.pow(2).sum()).item())
+    del x, y
+    return closure, info
+
+
+def evaluate(n_train: int = 512, snapshots: int = 64, n_eval: int = 1024, horizons=(5.0, 20.0, 50.0, 200.0),
+             train_steps: int = 3000, seed: int = 0, tau: float = 1e-3, segment: int = 50,
+             start_step: int = 0) -> dict:
+    """Train, then for each horizon tf solve the evaluation ensemble (n_eval
+    domains, 4096 fine cells) from t0 = start_step * 0.02 to t0 + tf four
+    ways -- fine FP64 (the judge), plain coarse, closure-corrected coarse, and
+    run_adaptive with tolerance tau -- and report wall times and the relative
+    L2 error of each against the coarse-grained judge."""
     torch = _torch()
     sw = _sw()
     solver = sw.Solver(0)
-    closure = Closure(solver, seed=seed)
-    out = {"fine_nx": FINE_NX, "coarse_nx": COARSE_NX, "n_train_traj": n_train, "snapshots": snapshots,
-           "n_eval": n_eval, "tf": tf, "t0": start_step * COARSE_DT}
-    t0 = time.perf_counter()
-    x, y = make_training_data(solver, closure, n_train, snapshots, interval=25, seed=seed + 1, spinup=CHAOS_SPINUP)
-    torch.cuda.synchronize()
-    out["datagen_s"] = time.perf_counter() - t0
-    out["output_scale"] = closure.calibrate(y)
-    t0 = time.perf_counter()
-    losses = closure.train(x, y, steps=train_steps, batch=64, lr=2e-3, seed=seed + 2)
-    torch.cuda.synchronize()
-    out["train_s"] = time.perf_counter() - t0
-    out["loss_first"], out["loss_last"] = float(losses[:10].mean()), float(losses[-50:].mean())
-    hx, hy = make_training_data(solver, closure, 32, 8, interval=25, seed=seed + 999, spinup=CHAOS_SPINUP)
-    out["heldout_defect_ratio"] = float(((hy - closure.infer(hx)).pow(2).sum() / hy.pow(2).sum()).item())
-    del x, y
-    fine = fine_ensemble(n_eval, seed=seed + 5)
+    closure, out = train_closure(solver, n_train, snapshots, train_steps, seed)
+    out.update({"fine_nx": FINE_NX, "coarse_nx": COARSE_NX, "n_eval": n_eval, "t0": start_step * COARSE_DT,
+                "tau": tau, "segment": segment, "horizons": []})
+    fine0 = fine_ensemble(n_eval, seed=seed + 5)
     if start_step:
-        advance_fine(solver, fine, start_step * FACTOR)
-    start = coarse_grain(solver, fine)
-    checkpoints = [t for t in (0.5, 1, 2, 5, 10, 20, 50, 100, 200) if t <= tf]
-    steps_at = [int(round(t / COARSE_DT)) for t in checkpoints]
-    errs = {"plain": [], "closure": []}
-    amax = {"plain": [], "closure": [], "judge": []}
-    judge = fine.clone()
-    t_fine = t_plain = t_clos = 0.0
-    u_plain, u_clos = start.clone(), start.clone()
-    prev = 0
-    fallbacks = 0
-    for t, s in zip(checkpoints, steps_at):
-        k = s - prev
-        prev = s
-        torch.cuda.synchronize()
-        a = time.perf_counter()
-        advance_fine(solver, judge, k * FACTOR)
-        torch.cuda.synchronize()
-        b = time.perf_counter()
-        closure.step(u_plain, k, use_closure=False)
-        torch.cuda.synchronize()
-        c = time.perf_counter()
-        if math.isinf(tau):
-            closure.step(u_clos, k, use_closure=True)
-        else:
-            fallbacks += run_with_fallback(solver, closure, u_clos, k, segment, tau)
-        torch.cuda.synchronize()
-        d = time.perf_counter()
-        t_fine += b - a
-        t_plain += c - b
-        t_clos += d - c
+        advance_fine(solver, fine0, start_step * FACTOR)
+    start = coarse_grain(solver, fine0)
+    # one-time costs (graph captures, FFT plans) out of the timings
+    advance_fine(solver, fine0.clone(), FACTOR)
+    closure.step(start.clone(), 1, use_closure=True)
+    closure.step(start.clone(), 1, use_closure=False)
+    run_adaptive(solver, closure, fine0, 2 * segment, segment, float("inf"))
+    for tf in horizons:
+        steps = int(round(tf / COARSE_DT))
+        judge = fine0.clone()
+        _, t_fine = _timed(lambda: advance_fine(solver, judge, steps * FACTOR))
         ref = coarse_grain(solver, judge)
-        errs["plain"].append(rel_l2(u_plain, ref))
-        errs["closure"].append(rel_l2(u_clos, ref))
-        for name, v in (("plain", u_plain), ("closure", u_clos), ("judge", ref)):
-            amax[name].append(float(v.abs().max().item()))
-    out.update({"checkpoints": checkpoints, "rel_l2_plain": errs["plain"], "rel_l2_closure": errs["closure"],
-                "max_abs_plain": amax["plain"], "max_abs_closure": amax["closure"], "max_abs_judge": amax["judge"],
-                "time_fine_s": t_fine, "time_plain_s": t_plain, "time_closure_s": t_clos,
-                "speedup_closure_vs_fine": t_fine / t_clos if t_clos else None, "fallbacks": fallbacks,
-                "tau": tau})
-
-    def horizon(e):
-        ok = [t for t, v in zip(checkpoints, e) if v <= 1e-3]
-        return max(ok) if ok and ok == checkpoints[:len(ok)] else (0.0 if not ok else ok[-1])
-
-    out["horizon_1e-3_plain"] = horizon(errs["plain"])
-    out["horizon_1e-3_closure"] = horizon(errs["closure"])
+        row = {"tf": tf, "time_fine_s": t_fine}
+        for name, on in (("plain", False), ("closure", True)):
+            v = start.clone()
+            _, row["time_%s_s" % name] = _timed(lambda: closure.step(v, steps, use_closure=on))
+            row["rel_l2_%s" % name] = rel_l2(v, ref)
+        (u, info), row["time_adaptive_s"] = _timed(lambda: run_adaptive(solver, closure, fine0, steps, segment, tau))
+        err = ((u.double() - ref.double()).norm(dim=1) / ref.double().norm(dim=1))
+        row["rel_l2_adaptive"] = float(err.mean().item())
+        row["max_rel_l2_adaptive"] = float(err.max().item())
+        row["fallback_domains"] = info["fallback"]
+        row["segments_closure"], row["segments_plain"] = info["closure"], info["plain"]
+        kept = info["estimate"] <= tau
+        if bool(kept.any()):
+            row["kept_mean_estimate"] = float(info["estimate"][kept].mean().item())
+            row["kept_mean_rel_l2"] = float(err[kept].mean().item())
+            row["kept_max_rel_l2"] = float(err[kept].max().item())
+        row["speedup_adaptive_vs_fine"] = t_fine / row["time_adaptive_s"]
+        out["horizons"].append(row)
     solver.close()
     return out
 
@@ -312,17 +366,19 @@ if __name__ == "__main__":
     import sys
     from pathlib import Path
     sys.path.insert(0, str(Path(__file__).resolve().parent.parent))
-    ap = argparse.ArgumentParser(description="train and evaluate the KS closure (config 5 shape)")
+    ap = argparse.ArgumentParser(description="train and evaluate the KS closure (1024 domains, coarse nx 1024)")
     ap.add_argument("--train-traj", type=int, default=512)
     ap.add_argument("--snapshots", type=int, default=64)
     ap.add_argument("--eval", type=int, default=1024)
-    ap.add_argument("--tf", type=float, default=200.0)
+    ap.add_argument("--horizons", default="5,20,50,200", help="comma-separated tf values")
     ap.add_argument("--train-steps", type=int, default=3000)
-    ap.add_argument("--tau", type=float, default=float("inf"))
-    ap.add_argument("--start-step", type=int, default=CHAOS_SPINUP, help="coarse steps of spin-up before t0")
+    ap.add_argument("--tau", type=float, default=1e-3)
+    ap.add_argument("--segment", type=int, default=50)
+    ap.add_argument("--start-step", type=int, default=0, help="coarse steps of spin-up before t0")
     ap.add_argument("--json", default=None)
     a = ap.parse_args()
-    res = evaluate(a.train_traj, a.snapshots, a.eval, a.tf, a.train_steps, tau=a.tau, start_step=a.start_step)
+    res = evaluate(a.train_traj, a.snapshots, a.eval, [float(t) for t in a.horizons.split(",")], a.train_steps,
+                   tau=a.tau, segment=a.segment, start_step=a.start_step)
     print(json.dumps(res, indent=1))
     if a.json:
         Path(a.json).write_text(json.dumps(res, indent=1))

@@ -235,13 +235,13 @@ struct Runner {
     int swept_segment(int64_t nd, int down_phase) {
         const int64_t nx = cfg.nx;
         if (persistent && ((nd + 1) & 1) == down_phase) {
-            SW_CUDA(ctx, ops->persistent(&p, cur, ctx->d_slots, ctx->d_flags, ctx->d_status, nx, W, nd, s));
+            SW_CUDA(ctx, ops->persistent(&p, cur, ctx->d_slots, ctx->d_flags, ctx->d_status, nx, W, cfg.threads, nd, s));
             ++launches;
             return SW_OK;
         }
-        SW_CUDA(ctx, ops->swept(&p, MODE_UP, 0, cur, ctx->d_slots, nx, W, s));
-        for (int64_t d = 1; d <= nd; ++d) SW_CUDA(ctx, ops->swept(&p, MODE_DIAMOND, (int)(d & 1), cur, ctx->d_slots, nx, W, s));
-        SW_CUDA(ctx, ops->swept(&p, MODE_DOWN, down_phase, cur, ctx->d_slots, nx, W, s));
+        SW_CUDA(ctx, ops->swept(&p, MODE_UP, 0, cur, ctx->d_slots, nx, W, cfg.threads, s));
+        for (int64_t d = 1; d <= nd; ++d) SW_CUDA(ctx, ops->swept(&p, MODE_DIAMOND, (int)(d & 1), cur, ctx->d_slots, nx, W, cfg.threads, s));
+        SW_CUDA(ctx, ops->swept(&p, MODE_DOWN, down_phase, cur, ctx->d_slots, nx, W, cfg.threads, s));
         launches += nd + 2;
         return SW_OK;
     }

@@ -328,7 +328,7 @@ int sw_query_tuning(sw_ctx *ctx, const sw_config *cfg, int32_t n, const int64_t 
         }
         return cudaMemcpy(tune_state, host.data(), host.size(), cudaMemcpyHostToDevice);
     };
-    const int maxt = (c.problem == SW_EULER) ? 256 : 1024;
+    const int maxt = ops->max_threads;
     int best = -1;
     for (int W = 32; W <= 1024; W *= 2) {
         if (!valid_tile(W, n, nx)) continue;

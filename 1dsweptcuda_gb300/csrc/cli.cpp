@@ -5,6 +5,13 @@
 // Euler1D_SweptShared.cu:1112-1287: the same row names and leading spaces,
 // ostream precision 10 for the solution (values printed in the run's
 // precision), default precision for the timing row.
+//
+// A solution path ending in ".npy" gets the same rows in binary instead: a
+// NumPy structured array of records (var int32, t float64, v REAL[n]), n = nx
+// (Euler nx - 2), rows in the .dat order with the .dat's values unrounded.
+// Record 0 is the header: var = -1, t = lx, v[0] = n, v[1] = dx, v[2] = the
+// problem (0 Heat, 1 KS, 2 Euler).  The var index is the row name's position
+// in Temperature | Velocity | Density, Velocity, Energy, Pressure.
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -82,13 +89,107 @@ struct Writer {
     }
 };
 
+// The .npy form of Writer: same rows, same values, unrounded binary records.
 template <typename R>
+struct NpyWriter {
+    std::FILE *f = nullptr;
+    int problem;
+    int alg;
+    const sw_constants &k;
+    int64_t nx;
+    int64_t n_rows = 0;
+    long shape_at = 0;
+    bool ok = true;
+    std::vector<R> buf;
+    static constexpr int kShapeWidth = 20;
+
+    int64_t n() const { return problem == SW_EULER ? nx - 2 : nx; }
+    R pressure(const R *q) const { return (R)k.mgam * (q[2] - ((R)0.5 * q[1] * q[1] / q[0])); }
+    R energy(const R *q) const {
+        R u = q[1] / q[0];
+        return q[2] / q[0] - (R)0.5 * u * u;
+    }
+
+    // NPY 1.0 header; the row count is patched in by finish()
+    bool open(const char *path) {
+        f = std::fopen(path, "wb");
+        if (!f) return false;
+        const char *real = sizeof(R) == 4 ? "<f4" : "<f8";
+        std::string h = "{'descr': [('var', '<i4'), ('t', '<f8'), ('v', '" + std::string(real) + "', (" +
+                        std::to_string(n()) + ",))], 'fortran_order': False, 'shape': (";
+        const size_t shape_off = h.size();
+        h += std::string(kShapeWidth, ' ') + ",), }";
+        while ((10 + h.size() + 1) % 64) h += ' ';
+        h += '\n';
+        const unsigned char magic[8] = {0x93, 'N', 'U', 'M', 'P', 'Y', 1, 0};
+        const uint16_t len = (uint16_t)h.size();
+        const unsigned char lenb[2] = {(unsigned char)(len & 0xff), (unsigned char)(len >> 8)};
+        ok = std::fwrite(magic, 1, 8, f) == 8 && std::fwrite(lenb, 1, 2, f) == 2 &&
+             std::fwrite(h.data(), 1, h.size(), f) == h.size();
+        shape_at = (long)(10 + shape_off);
+        buf.assign((size_t)n(), R(0));
+        return ok;
+    }
+    void record(int32_t var, double t, const R *v) {
+        unsigned char hdr[12];
+        std::memcpy(hdr, &var, 4);
+        std::memcpy(hdr + 4, &t, 8);
+        ok = ok && std::fwrite(hdr, 1, 12, f) == 12 && std::fwrite(v, sizeof(R), (size_t)n(), f) == (size_t)n();
+        ++n_rows;
+    }
+    // one Euler row of derived values from the device-layout-free host state (3 per cell)
+    void euler_row(int var, double t, const R *u, bool ic) {
+        for (int64_t i = 1; i < nx - 1; ++i) {
+            const R *q = u + 3 * i;
+            R val;
+            if (var == 0) val = q[0];
+            else if (var == 1) val = ic ? q[1] : q[1] / q[0];  // the IC row holds rho*u (as the .dat)
+            else if (var == 2) val = ic ? q[2] / q[0] : energy(q);
+            else val = pressure(q);
+            buf[(size_t)(i - 1)] = val;
+        }
+        record(var, t, buf.data());
+    }
+    void head(const R *ic) {
+        std::fill(buf.begin(), buf.end(), R(0));
+        buf[0] = (R)n();
+        buf[1] = (R)k.dx;
+        buf[2] = (R)problem;
+        record(-1, problem == SW_EULER ? (double)(R)k.lx : k.lx, buf.data());
+        rows_of(ic, 0.0, true);
+    }
+    void rows_of(const R *u, double t, bool ic) {
+        if (problem == SW_EULER) {
+            for (int v = 0; v < 4; ++v) euler_row(v, t, u, ic);
+        } else {
+            record(0, t, u);
+        }
+    }
+    void rows(const R *u, double t, bool, bool) { rows_of(u, t, false); }
+    bool good() const { return ok; }
+    bool finish() {
+        if (!f) return false;
+        std::string num = std::to_string(n_rows);
+        num = std::string(kShapeWidth - num.size(), ' ') + num;
+        ok = ok && std::fseek(f, shape_at, SEEK_SET) == 0 && std::fwrite(num.data(), 1, num.size(), f) == num.size();
+        ok = (std::fclose(f) == 0) && ok;
+        f = nullptr;
+        return ok;
+    }
+};
+
+template <typename R>
+bool writer_good(const Writer<R> &w) { return w.f.good(); }
+template <typename R>
+bool writer_good(const NpyWriter<R> &w) { return w.good(); }
+
+template <typename R, typename W>
 int snapshot_cb(void *user, double t, const void *state, int64_t) {
-    Writer<R> *w = static_cast<Writer<R> *>(user);
+    W *w = static_cast<W *>(user);
     // Heat/KS classic rows start with a space; swept Heat rows do not; KS always does.
     const bool lead = (w->problem == SW_KS) || (w->problem == SW_HEAT && w->alg == SW_ALG_CLASSIC);
     w->rows(static_cast<const R *>(state), t, lead, true);
-    return w->f.good() ? 0 : 1;
+    return writer_good(*w) ? 0 : 1;
 }
 
 const char *scheme_banner(int problem, int alg) {
@@ -126,6 +227,47 @@ int selftest(sw_ctx *ctx, sw_config cfg, const std::vector<R> &ic) {
         else std::cout << "NOT EQUAL!" << std::endl << bad << " out of " << a.size() << std::endl;
     }
     return -1;
+}
+
+template <typename R, typename W>
+int run_and_write(W &w, sw_config cfg, const std::vector<R> &ic, std::vector<R> &fin, int argc, char **argv) {
+    const int problem = cfg.problem;
+    sw_ctx *ctx = nullptr;
+    int rc = sw_ctx_create(0, &ctx);
+    if (rc) {
+        std::cout << "CUDA error: " << sw_strerror(rc) << std::endl;
+        return rc;
+    }
+    if (cfg.alg == SW_ALG_SELFTEST) {
+        rc = selftest<R>(ctx, cfg, ic);
+        sw_ctx_destroy(ctx);
+        return rc;
+    }
+    std::cout << scheme_banner(problem, cfg.alg) << std::endl;
+    sw_result res{};
+    rc = sw_run(ctx, &cfg, ic.data(), fin.data(), snapshot_cb<R, W>, &w, &res);
+    if (rc) {
+        std::cout << "CUDA error: " << sw_ctx_last_error(ctx) << std::endl;
+        sw_ctx_destroy(ctx);
+        return rc;
+    }
+    sw_ctx_destroy(ctx);
+
+    const double t_end = cfg.tf - 0.25 * cfg.dt;
+    std::cout << res.t_final << " " << t_end << std::endl;
+    double n_timesteps = res.t_final / cfg.dt;
+    if (problem == SW_KS) n_timesteps = (double)(int)n_timesteps;
+    std::cout << n_timesteps << " timesteps" << std::endl;
+    std::cout << "Averaged " << res.us_per_step << " microseconds (us) per timestep" << std::endl;
+
+    if (argc > 8) {  // the reference opens argv[8] whenever argc > 7; argv[8] is NULL when argc == 8
+        std::ofstream ftime(argv[8], std::ios::app);
+        if (!ftime) return SW_ERR_IO;
+        ftime << cfg.nx << "\t" << cfg.tpb << "\t" << res.us_per_step << std::endl;
+    }
+    // final rows: Heat without a trailing newline (Heat1D_SweptShared.cu:821-824)
+    w.rows(fin.data(), res.t_final, problem == SW_KS, problem != SW_HEAT);
+    return writer_good(w) ? SW_OK : SW_ERR_IO;
 }
 
 template <typename R>
@@ -177,6 +319,19 @@ int cli(int problem, int argc, char **argv) {
     std::vector<R> ic((size_t)cfg.nx * comps), fin((size_t)cfg.nx * comps);
     sw_initial_condition(&cfg, ic.data());
 
+    const std::string out_path = argv[7];
+    const bool npy = out_path.size() >= 4 && out_path.compare(out_path.size() - 4, 4, ".npy") == 0;
+    if (npy) {
+        NpyWriter<R> w{nullptr, problem, cfg.alg, k, cfg.nx};
+        if (!w.open(argv[7])) {
+            std::cout << "cannot open " << argv[7] << std::endl;
+            return SW_ERR_IO;
+        }
+        w.head(ic.data());
+        rc = run_and_write<R>(w, cfg, ic, fin, argc, argv);
+        const bool written = w.finish();
+        return rc ? rc : (written ? SW_OK : SW_ERR_IO);
+    }
     std::ofstream fwr(argv[7], std::ios::trunc);
     if (!fwr) {
         std::cout << "cannot open " << argv[7] << std::endl;
@@ -185,44 +340,9 @@ int cli(int problem, int argc, char **argv) {
     fwr.precision(10);
     Writer<R> w{fwr, problem, cfg.alg, k, cfg.nx};
     w.head(ic.data());
-
-    sw_ctx *ctx = nullptr;
-    rc = sw_ctx_create(0, &ctx);
-    if (rc) {
-        std::cout << "CUDA error: " << sw_strerror(rc) << std::endl;
-        return rc;
-    }
-    if (cfg.alg == SW_ALG_SELFTEST) {
-        rc = selftest<R>(ctx, cfg, ic);
-        sw_ctx_destroy(ctx);
-        return rc;
-    }
-    std::cout << scheme_banner(problem, cfg.alg) << std::endl;
-    sw_result res{};
-    rc = sw_run(ctx, &cfg, ic.data(), fin.data(), snapshot_cb<R>, &w, &res);
-    if (rc) {
-        std::cout << "CUDA error: " << sw_ctx_last_error(ctx) << std::endl;
-        sw_ctx_destroy(ctx);
-        return rc;
-    }
-    sw_ctx_destroy(ctx);
-
-    const double t_end = cfg.tf - 0.25 * cfg.dt;
-    std::cout << res.t_final << " " << t_end << std::endl;
-    double n_timesteps = res.t_final / cfg.dt;
-    if (problem == SW_KS) n_timesteps = (double)(int)n_timesteps;
-    std::cout << n_timesteps << " timesteps" << std::endl;
-    std::cout << "Averaged " << res.us_per_step << " microseconds (us) per timestep" << std::endl;
-
-    if (argc > 8) {  // the reference opens argv[8] whenever argc > 7; argv[8] is NULL when argc == 8
-        std::ofstream ftime(argv[8], std::ios::app);
-        if (!ftime) return SW_ERR_IO;
-        ftime << cfg.nx << "\t" << cfg.tpb << "\t" << res.us_per_step << std::endl;
-    }
-    // final rows: Heat without a trailing newline (Heat1D_SweptShared.cu:821-824)
-    w.rows(fin.data(), res.t_final, problem == SW_KS, problem != SW_HEAT);
+    rc = run_and_write<R>(w, cfg, ic, fin, argc, argv);
     fwr.close();
-    return fwr.fail() ? SW_ERR_IO : SW_OK;
+    return rc ? rc : (fwr.fail() ? SW_ERR_IO : SW_OK);
 }
 
 }  // namespace

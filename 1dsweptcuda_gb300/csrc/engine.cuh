@@ -47,13 +47,19 @@ struct Scheme {
     static constexpr int R = (P == SW_HEAT) ? 1 : 2;
     static constexpr int S = (P == SW_HEAT) ? 1 : 2;
     static constexpr int C = (P == SW_EULER) ? 3 : 1;
-    // threads per block: one per cell for Heat/KS; Euler caps at 256 so its
-    // long stencil keeps its registers (a thread then walks W/256 cells)
-    static constexpr int MAXT = (P == SW_EULER) ? 256 : 1024;
+    // largest swept block: 512 threads for Heat/KS (a 1024-thread bound would
+    // cap the FP64 kernels at 32 registers and spill), 256 for Euler so its
+    // long stencil keeps its registers
+    static constexpr int MAXT = (P == SW_EULER) ? 256 : 512;
+    // largest classic block (one cell per thread, any block size gives the same result)
+    static constexpr int CMAXT = (P == SW_EULER) ? 256 : 1024;
     using G = typename std::conditional<P == SW_EULER, V4<T>, T>::type;
 };
 
-// ---- shared-memory tile access: layout [row][component][L], L = W + 2R
+// ---- shared-memory tile access: layout [row][component][L], cell x of a row at
+// index R + x.  L = W + 8 (>= W + 2R): every row starts 16-byte aligned and the
+// 8-value windows of the 4-cells-per-thread path never leave their row.
+__host__ __device__ constexpr int row_stride(int W) { return W + 8; }
 template <int P, typename T>
 __device__ __forceinline__ void tile_put(T *rows, int L, int row, int x, const typename Scheme<P, T>::G &v) {
     constexpr int R = Scheme<P, T>::R;
@@ -135,7 +141,7 @@ __device__ __forceinline__ void tile_point(const Params<T> &p, T *rows, int L, i
 
 template <int P, typename T>
 __host__ __device__ constexpr size_t swept_smem_bytes(int W) {
-    return sizeof(T) * 2 * Scheme<P, T>::C * (size_t)(W + 2 * Scheme<P, T>::R);
+    return sizeof(T) * 2 * Scheme<P, T>::C * (size_t)row_stride(W);
 }
 
 __device__ __forceinline__ int64_t wrap_pos(int64_t q, int64_t nx) {
@@ -197,12 +203,98 @@ __device__ __forceinline__ void tile_export(const T *rows, int L, int W, typenam
     }
 }
 
+// Aligned 4-value shared-memory loads.
+__device__ __forceinline__ void load4(const float *p, float *w) {
+    const float4 v = *reinterpret_cast<const float4 *>(p);
+    w[0] = v.x; w[1] = v.y; w[2] = v.z; w[3] = v.w;
+}
+__device__ __forceinline__ void load4(const double *p, double *w) {
+    const double2 a = *reinterpret_cast<const double2 *>(p);
+    const double2 b = *reinterpret_cast<const double2 *>(p + 2);
+    w[0] = a.x; w[1] = a.y; w[2] = b.x; w[3] = b.y;
+}
+// Four values as two aligned pairs (8-byte aligned float, 16-byte aligned double).
+__device__ __forceinline__ void load_pairs(const float *p, float *w) {
+    const float2 a = *reinterpret_cast<const float2 *>(p);
+    const float2 b = *reinterpret_cast<const float2 *>(p + 2);
+    w[0] = a.x; w[1] = a.y; w[2] = b.x; w[3] = b.y;
+}
+__device__ __forceinline__ void load_pairs(const double *p, double *w) { load4(p, w); }
+__device__ __forceinline__ void store_pairs(float *p, const float *w) {
+    *reinterpret_cast<float2 *>(p) = make_float2(w[0], w[1]);
+    *reinterpret_cast<float2 *>(p + 2) = make_float2(w[2], w[3]);
+}
+__device__ __forceinline__ void store_pairs(double *p, const double *w) {
+    *reinterpret_cast<double2 *>(p) = make_double2(w[0], w[1]);
+    *reinterpret_cast<double2 *>(p + 2) = make_double2(w[2], w[3]);
+}
+
+// Heat / KS with 4 consecutive cells per thread (blockDim.x == W / 4, 0 <= lo <
+// hi <= W).  The live range [lo, hi) is packed onto the lowest threads from the
+// 4-aligned cell below lo, so that as a triangle narrows whole warps fall idle
+// instead of every warp running part-empty.  The thread reads the 8-value
+// window of source cells x0 - R .. x0 + 7 - R with two aligned vector loads and
+// updates those of its cells x0 .. x0 + 3 that lie in [lo, hi).  Same
+// arithmetic as tile_point, cell for cell.
+template <int P, typename T>
+__device__ __forceinline__ void tile_span4(const Params<T> &p, T *rows, int L, int par, int lo, int hi, Ends e) {
+    constexpr int R = Scheme<P, T>::R;
+    const int x0 = (lo & ~3) + (int)threadIdx.x * 4;
+    if (x0 >= hi) return;
+    const T *src = rows + (par ^ 1) * L;
+    T *dst = rows + par * L + R;
+    T w[8];
+    load4(src + x0, w);  // cell x0 - R + k at src[R + x0 - R + k] = src[x0 + k]
+    load4(src + x0 + 4, w + 4);
+    // All four cells are computed (their windows lie inside the row; values of
+    // cells outside [lo, hi) are never stored), so the warps at a triangle's
+    // edge run the same instructions as the rest; only the stores branch.
+    T o[4];
+    if constexpr (P == SW_KS) {
+        if (par) {
+#pragma unroll
+            for (int i = 0; i < 4; ++i) o[i] = ks_predict(p, w[i], w[i + 1], w[i + 2], w[i + 3], w[i + 4]);
+        } else {
+            T d[4];
+            load_pairs(dst + x0, d);  // dst + x0 = row + 2 + x0: 8-byte aligned for float, 16 for double
+#pragma unroll
+            for (int i = 0; i < 4; ++i) o[i] = ks_correct(p, d[i], w[i], w[i + 1], w[i + 2], w[i + 3], w[i + 4]);
+        }
+        if (x0 >= lo && x0 + 4 <= hi) {
+            store_pairs(dst + x0, o);
+            return;
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            T l = w[i], c = w[i + 1], r = w[i + 2];
+            if (p.bc != SW_BC_PERIODIC) {  // insulated ends, Heat1D_SweptShared.cu:140-142,352-353
+                if (x0 + i == e.first) l = r;
+                if (x0 + i == e.last) r = l;
+            }
+            o[i] = heat_step(p, l, c, r);
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+        if (x0 + i >= lo && x0 + i < hi) dst[x0 + i] = o[i];
+}
+
 // Down part: sub-steps j = 1..H on the growing centre [W/2 - jR, W/2 + jR).
 template <int P, typename T>
 __device__ __forceinline__ void tile_down(const Params<T> &p, T *rows, int L, int W, int64_t base) {
     constexpr int R = Scheme<P, T>::R;
     const int h = W >> 1, H = W / (2 * R);
     const Ends e = tile_ends(base, p.nx, W, R);
+    if constexpr (P != SW_EULER) {
+        if ((int)blockDim.x * 4 == W) {
+            for (int j = 1; j <= H; ++j) {
+                tile_span4<P, T>(p, rows, L, j & 1, h - j * R, h + j * R, e);
+                __syncthreads();
+            }
+            return;
+        }
+    }
     for (int j = 1; j <= H; ++j) {
         for (int x = threadIdx.x; x < W; x += blockDim.x)
             if (x >= h - j * R && x < h + j * R) tile_point<P, T>(p, rows, L, j & 1, x, e);
@@ -215,11 +307,38 @@ __device__ __forceinline__ void tile_up(const Params<T> &p, T *rows, int L, int 
     constexpr int R = Scheme<P, T>::R;
     const int H = W / (2 * R);
     const Ends e = tile_ends(base, p.nx, W, R);
+    if constexpr (P != SW_EULER) {
+        if ((int)blockDim.x * 4 == W) {
+            for (int u = 1; u < H; ++u) {
+                tile_span4<P, T>(p, rows, L, u & 1, u * R, W - u * R, e);
+                __syncthreads();
+            }
+            return;
+        }
+    }
     for (int u = 1; u < H; ++u) {
         for (int x = threadIdx.x; x < W; x += blockDim.x)
             if (x >= u * R && x < W - u * R) tile_point<P, T>(p, rows, L, u & 1, x, e);
         __syncthreads();
     }
+}
+
+// Default threads per swept block.  FP32 Heat / KS run 4 contiguous cells per
+// thread from 128-cell tiles up (the vector path), FP64 one cell per thread
+// (two on 1024-cell tiles): the FP64 pipe, not shared memory, bounds FP64 and
+// it wants the warps.  Euler walks W / 256 cells.
+template <int P, typename T>
+__host__ __device__ constexpr int swept_threads(int W) {
+    if (P == SW_EULER) return W < Scheme<P, T>::MAXT ? W : Scheme<P, T>::MAXT;
+    if (sizeof(T) == 4) return W >= 128 ? W / 4 : W;
+    return W <= Scheme<P, T>::MAXT ? W : Scheme<P, T>::MAXT;
+}
+
+// threads per swept block for a request (0 or out of range = the default)
+template <int P, typename T>
+inline int swept_threads_for(int W, int threads) {
+    if (threads < 32 || threads > Scheme<P, T>::MAXT || threads > W || (threads & 31)) return swept_threads<P, T>(W);
+    return threads;
 }
 
 // One swept pass of tile t of a periodic / bounded domain of p.nx cells whose
@@ -231,7 +350,7 @@ __device__ __forceinline__ void swept_tile(const Params<T> &p, typename Scheme<P
                                            typename Scheme<P, T>::G *__restrict__ slots, T *rows, const int W,
                                            const int phase, const int64_t t) {
     constexpr int R = Scheme<P, T>::R;
-    const int L = W + 2 * R, h = W >> 1;
+    const int L = row_stride(W), h = W >> 1;
     const int64_t nx = p.nx, nhalf = nx / h;
     const int64_t base = t * W + (int64_t)phase * h;
     const int64_t hl = (2 * t + phase) % nhalf;
@@ -284,13 +403,18 @@ __device__ __forceinline__ void classic_cell(const Params<T> &p, const typename 
         }
         out[g] = heat_step(p, in[l], in[g], in[r]);
     } else if constexpr (P == SW_KS) {
-        int64_t i[5];
+        T v[5];
+        if (g >= 2 && g < nx - 2) {  // interior: no wrap
 #pragma unroll
-        for (int k = 0; k < 5; ++k) i[k] = wrap_pos(g - 2 + k, nx);
+            for (int k = 0; k < 5; ++k) v[k] = in[g - 2 + k];
+        } else {
+#pragma unroll
+            for (int k = 0; k < 5; ++k) v[k] = in[wrap_pos(g - 2 + k, nx)];
+        }
         if (sub == 0)
-            out[g] = ks_predict(p, in[i[0]], in[i[1]], in[i[2]], in[i[3]], in[i[4]]);
+            out[g] = ks_predict(p, v[0], v[1], v[2], v[3], v[4]);
         else
-            out[g] = ks_correct(p, out[g], in[i[0]], in[i[1]], in[i[2]], in[i[3]], in[i[4]]);
+            out[g] = ks_correct(p, out[g], v[0], v[1], v[2], v[3], v[4]);
     } else {
         if (g == 0 || g == nx - 1) {
             const int side = (g == 0) ? 0 : 1;
@@ -318,7 +442,7 @@ __device__ __forceinline__ void classic_cell(const Params<T> &p, const typename 
 }
 
 template <int P, typename T>
-__global__ void __launch_bounds__(Scheme<P, T>::MAXT) k_classic(const Params<T> p, const typename Scheme<P, T>::G *__restrict__ in,
+__global__ void __launch_bounds__(Scheme<P, T>::CMAXT) k_classic(const Params<T> p, const typename Scheme<P, T>::G *__restrict__ in,
                                                   typename Scheme<P, T>::G *__restrict__ out, const int sub) {
     const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (g < p.nx) classic_cell<P, T>(p, in, out, sub, g);
@@ -352,7 +476,7 @@ cudaError_t launch_classic(const void *vp, const void *in, void *out, int sub, i
                            cudaStream_t s) {
     using G = typename Scheme<P, T>::G;
     const Params<T> &p = *static_cast<const Params<T> *>(vp);
-    if (block <= 0 || block > Scheme<P, T>::MAXT) block = block <= 0 ? 256 : Scheme<P, T>::MAXT;
+    if (block <= 0 || block > Scheme<P, T>::CMAXT) block = block <= 0 ? 256 : Scheme<P, T>::CMAXT;
     const int64_t grid = (nx + block - 1) / block;
     k_classic<P, T><<<(unsigned)grid, block, 0, s>>>(p, static_cast<const G *>(in), static_cast<G *>(out), sub);
     return cudaGetLastError();
@@ -360,7 +484,7 @@ cudaError_t launch_classic(const void *vp, const void *in, void *out, int sub, i
 
 template <int P, typename T>
 cudaError_t launch_swept(const void *vp, int mode, int phase, void *state, void *slots, int64_t nx, int W,
-                         cudaStream_t s) {
+                         int threads_req, cudaStream_t s) {
     using G = typename Scheme<P, T>::G;
     static bool configured = false;
     if (!configured) {
@@ -372,7 +496,7 @@ cudaError_t launch_swept(const void *vp, int mode, int phase, void *state, void 
     const Params<T> &p = *static_cast<const Params<T> *>(vp);
     const size_t smem = swept_smem_bytes<P, T>(W);
     const unsigned grid = (unsigned)(nx / W);
-    const int threads = W < Scheme<P, T>::MAXT ? W : Scheme<P, T>::MAXT;
+    const int threads = swept_threads_for<P, T>(W, threads_req);
     G *st = static_cast<G *>(state), *sl = static_cast<G *>(slots);
     switch (mode) {
     case MODE_UP: k_swept<P, T, MODE_UP><<<grid, threads, smem, s>>>(p, st, sl, W, phase); break;

@@ -14,6 +14,7 @@ Ops make_ops() {
     o.S = Sc::S;
     o.C = 3;
     o.cell = sizeof(typename Sc::G);
+    o.max_threads = Sc::MAXT;
     o.classic = launch_classic<SW_EULER, T>;
     o.swept = launch_swept<SW_EULER, T>;
     o.persistent = launch_persistent<SW_EULER, T>;

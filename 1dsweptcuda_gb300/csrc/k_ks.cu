@@ -14,6 +14,7 @@ Ops make_ops() {
     o.S = Sc::S;
     o.C = 1;
     o.cell = sizeof(typename Sc::G);
+    o.max_threads = Sc::MAXT;
     o.classic = launch_classic<SW_KS, T>;
     o.swept = launch_swept<SW_KS, T>;
     o.persistent = launch_persistent<SW_KS, T>;

@@ -62,10 +62,10 @@ int run(const sw_config &c, void *state, cudaStream_t s) {
     const int64_t q = W / (2 * ops->R * ops->S);
     const int64_t full = c.n_steps / q, rem = c.n_steps - full * q;
     if (full >= 1) {
-        if (ops->swept(&p, MODE_UP, 0, state, slots, nx, W, s) != cudaSuccess) return SW_ERR_CUDA;
+        if (ops->swept(&p, MODE_UP, 0, state, slots, nx, W, c.threads, s) != cudaSuccess) return SW_ERR_CUDA;
         for (int64_t d = 1; d < full; ++d)
-            if (ops->swept(&p, MODE_DIAMOND, (int)(d & 1), state, slots, nx, W, s) != cudaSuccess) return SW_ERR_CUDA;
-        if (ops->swept(&p, MODE_DOWN, (int)(full & 1), state, slots, nx, W, s) != cudaSuccess) return SW_ERR_CUDA;
+            if (ops->swept(&p, MODE_DIAMOND, (int)(d & 1), state, slots, nx, W, c.threads, s) != cudaSuccess) return SW_ERR_CUDA;
+        if (ops->swept(&p, MODE_DOWN, (int)(full & 1), state, slots, nx, W, c.threads, s) != cudaSuccess) return SW_ERR_CUDA;
     }
     void *cur = state, *alt = work;
     for (int64_t i = 0; i < rem; ++i) {

@@ -101,7 +101,7 @@ __device__ __forceinline__ bool persistent_tile(const Params<T> &p, typename Sch
                                                 typename Scheme<P, T>::G *__restrict__ slots, unsigned *flags,
                                                 int *status, T *rows, const int W, const int64_t q,
                                                 const int64_t last, const int64_t t) {
-    const int L = W + 2 * Scheme<P, T>::R, h = W >> 1;
+    const int L = row_stride(W), h = W >> 1;
     const int64_t nx = p.nx, nhalf = nx / h;
     const int phase = (int)(q & 1);
     const int64_t base = t * W + (int64_t)phase * h;
@@ -207,7 +207,7 @@ __global__ void __launch_bounds__(Scheme<P, T>::MAXT)
 
 template <int P, typename T>
 cudaError_t launch_persistent(const void *vp, void *state, void *slots, unsigned *flags, int *status, int64_t nx,
-                              int W, int64_t n_diamonds, cudaStream_t s) {
+                              int W, int threads_req, int64_t n_diamonds, cudaStream_t s) {
     using G = typename Scheme<P, T>::G;
     static bool configured = false;
     auto kern = k_persistent<P, T>;
@@ -219,7 +219,7 @@ cudaError_t launch_persistent(const void *vp, void *state, void *slots, unsigned
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int threads = W < Scheme<P, T>::MAXT ? W : Scheme<P, T>::MAXT;
+    const int threads = swept_threads_for<P, T>(W, threads_req);
     cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) return cudaErrorInvalidConfiguration;
@@ -250,7 +250,7 @@ cudaError_t launch_swept_batch(const void *vp, int mode, int phase, void *state,
     }
     const Params<T> &p = *static_cast<const Params<T> *>(vp);
     const BatchDev &b = *static_cast<const BatchDev *>(bt);
-    if (threads <= 0 || threads > Scheme<P, T>::MAXT) threads = W < Scheme<P, T>::MAXT ? W : Scheme<P, T>::MAXT;
+    threads = swept_threads_for<P, T>(W, threads);
     const size_t smem = swept_smem_bytes<P, T>(W);
     G *st = static_cast<G *>(state), *sl = static_cast<G *>(slots);
     const unsigned grid = (unsigned)b.n_tiles;
@@ -268,7 +268,7 @@ cudaError_t launch_classic_batch(const void *vp, const void *in, void *out, int 
     using G = typename Scheme<P, T>::G;
     const Params<T> &p = *static_cast<const Params<T> *>(vp);
     const BatchDev &b = *static_cast<const BatchDev *>(bt);
-    if (block <= 0 || block > Scheme<P, T>::MAXT) block = 256;
+    if (block <= 0 || block > Scheme<P, T>::CMAXT) block = 256;
     const int64_t grid = (b.n_cells + block - 1) / block;
     k_classic_batch<P, T><<<(unsigned)grid, block, 0, s>>>(p, static_cast<const G *>(in), static_cast<G *>(out), b,
                                                             sub);
@@ -288,7 +288,7 @@ cudaError_t launch_persistent_batch(const void *vp, void *state, void *slots, co
         allow_big_smem(kern);
         configured = true;
     }
-    if (threads <= 0 || threads > Scheme<P, T>::MAXT) threads = W < Scheme<P, T>::MAXT ? W : Scheme<P, T>::MAXT;
+    threads = swept_threads_for<P, T>(W, threads);
     const BatchDev &b = *static_cast<const BatchDev *>(bt);
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);

@@ -47,22 +47,24 @@ struct Ops {
     int S;           // sub-steps per time step
     int C;           // state components per cell on the host (1 or 3)
     size_t cell;     // bytes per cell in device layout
+    int max_threads; // largest threads per block a swept kernel is built for
     // one classic sub-step (sub 0: predictor / heat step, 1: corrector)
     cudaError_t (*classic)(const void *params, const void *in, void *out, int sub, int64_t nx, int block,
                            cudaStream_t s);
-    // one swept launch over all tiles of width W at `phase` (0 aligned, 1 shifted by W/2)
+    // one swept launch over all tiles of width W at `phase` (0 aligned, 1 shifted by W/2);
+    // `threads` per block, 0 (or out of range) = the default for W
     cudaError_t (*swept)(const void *params, int mode, int phase, void *state, void *slots, int64_t nx, int W,
-                         cudaStream_t s);
+                         int threads, cudaStream_t s);
     // persistent swept variant: up-triangle, n_diamonds diamonds and the down-triangle in
     // one cooperative launch with per-half-tile phase flags; *status set non-zero on timeout.
     cudaError_t (*persistent)(const void *params, void *state, void *slots, unsigned *flags, int *status,
-                              int64_t nx, int W, int64_t n_diamonds, cudaStream_t s);
+                              int64_t nx, int W, int threads, int64_t n_diamonds, cudaStream_t s);
     // Euler host layout (3 per cell) <-> device layout (4 per cell); null for Heat/KS
     cudaError_t (*pack)(const void *in3, void *out4, int64_t nx, cudaStream_t s);
     cudaError_t (*unpack)(const void *in4, void *out3, int64_t nx, cudaStream_t s);
     // dynamic shared memory a swept block of width W needs
     size_t (*swept_smem)(int W);
-    // ensembles: `batch` points at a BatchDev (device tables), `threads` per block (0 = W)
+    // ensembles: `batch` points at a BatchDev (device tables), `threads` per block (0 = the default for W)
     cudaError_t (*batch_swept)(const void *params, int mode, int phase, void *state, void *slots, const void *batch,
                                int W, int threads, cudaStream_t s);
     cudaError_t (*batch_classic)(const void *params, const void *in, void *out, int sub, const void *batch, int block,

@@ -7,6 +7,9 @@
 * ``Perform``: the timing .txt file (header row, then ``nx tpb us_per_step``
   rows), pivoted nx x tpb like ``pyAnalysisTools/main_help.py`` ``Perform``
   (:14-25).
+* ``read_snapshots``: the binary form the programs write when the solution
+  path ends in ``.npy`` (a NumPy structured array, record 0 the header); the
+  same rows as the .dat, unrounded.  ``read_dat`` and ``Solved`` take either.
 """
 from __future__ import annotations
 
@@ -16,8 +19,27 @@ from pathlib import Path
 import numpy as np
 
 
+ROW_NAMES = {0: ["Temperature"], 1: ["Velocity"], 2: ["Density", "Velocity", "Energy", "Pressure"]}
+
+
+def read_snapshots(path) -> tuple[list[str], list]:
+    """A .npy solution file -> (header fields [lx, nx, dx] as text, rows of
+    (name, t, values)), the same shape as read_dat's result.  Values keep the
+    run's precision (float32 or float64)."""
+    a = np.load(path)
+    if a.dtype.names != ("var", "t", "v") or len(a) == 0 or int(a[0]["var"]) != -1:
+        raise ValueError("%s is not a swept1d snapshot file" % path)
+    h = a[0]
+    n, dx, problem = int(h["v"][0]), float(h["v"][1]), int(h["v"][2])
+    names = ROW_NAMES[problem]
+    rows = [(names[int(r["var"])], float(r["t"]), r["v"]) for r in a[1:]]
+    return [repr(float(h["t"])), str(n), repr(dx)], rows
+
+
 def read_dat(path) -> tuple[list[str], dict]:
     """Return (header fields, rows) with rows = list of (name, t, values)."""
+    if str(path).endswith(".npy"):
+        return read_snapshots(path)
     with open(path) as f:
         lines = f.read().splitlines()
     head = lines[0].split()

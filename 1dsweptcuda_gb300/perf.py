@@ -2,11 +2,14 @@
 time classic, swept and variant over problems, precisions, nx and tpb with the
 state resident on the device, and check that all paths agree bit for bit.
 
-    python 1dsweptcuda_gb300/perf.py [--quick] [--json out.json]
+    python 1dsweptcuda_gb300/perf.py [--quick] [--ensemble] [--only TEXT] [--precision 4|8]
+                                     [--threads 0,64,...] [--json out.json]
 
 Each case runs SW_TIME_STEPS with a step count that is a whole number of swept
 cycles for every tpb in the case, timed with CUDA events inside the library
 (sw_result.kernel_ms).  Prints one row per case and the swept/classic ratio.
+--threads times swept and variant at each listed threads per block (0 = the
+library's default for the tile width).
 """
 from __future__ import annotations
 
@@ -82,54 +85,62 @@ def main():
     ap.add_argument("--quick", action="store_true")
     ap.add_argument("--ensemble", action="store_true", help="also run the ensemble (config 4) rows")
     ap.add_argument("--json", default=None)
+    ap.add_argument("--only", default=None, help="run only cases whose label contains one of these comma-separated texts")
+    ap.add_argument("--precision", type=int, default=None, choices=[4, 8], help="run only this precision")
+    ap.add_argument("--threads", default="0", help="comma-separated threads per swept block (0 = default)")
     args = ap.parse_args()
     sw = importlib.import_module("1dsweptcuda_gb300")
     solver = sw.Solver(0)
     stream = torch.cuda.current_stream()
+    thread_list = [int(t) for t in args.threads.split(",")]
     rows = []
     for label, prob, prec, bc, nx, tpbs, steps, dt in cases(args.quick):
-        dtype = torch.float64 if prec == 8 else torch.float32
+        if (args.only and not any(o in label for o in args.only.split(","))) or \
+                (args.precision and args.precision != prec):
+            continue
         results = {}
-        for tpb in tpbs:
-            for alg in (sw.ALG_CLASSIC, sw.ALG_SWEPT, sw.ALG_VARIANT):
-                if alg == sw.ALG_CLASSIC and tpb != tpbs[0]:
-                    continue
-                cfg = sw.make_config(prob, prec, alg=alg, nx=nx, tpb=tpb, dt=dt, bc=bc,
-                                     time_mode=sw.TIME_STEPS, n_steps=steps)
-                ic = sw.initial_condition(cfg)
-                if prob == 2:
-                    dev = np.zeros((nx, 4), dtype=ic.dtype)
-                    dev[:, :3] = ic.reshape(-1, 3)
-                    ic = dev.ravel()
-                elif prob == 0 and bc == 2:
-                    x = np.arange(nx)
-                    ic = (50 + 100 * np.sin(2 * np.pi * x / nx)).astype(ic.dtype)
-                st = torch.from_numpy(ic).cuda()
-                solver.run_device(cfg, st.data_ptr(), stream.cuda_stream)  # warm
-                st = torch.from_numpy(ic).cuda()
-                torch.cuda.synchronize()
-                res = solver.run_device(cfg, st.data_ptr(), stream.cuda_stream)
-                out = st.cpu().numpy()
-                ups = nx * steps / (res.kernel_ms * 1e-3)
-                key = ("classic" if alg == 0 else "swept" if alg == 1 else "variant", tpb)
-                results[key] = (ups, out, res)
-                row = {"case": label, "precision": prec, "alg": key[0], "tpb": tpb if alg else None,
-                       "tile": res.tile, "nx": nx, "steps": steps, "ms": res.kernel_ms,
-                       "cell_updates_per_s": ups, "launches": res.launches,
-                       "finite": bool(np.isfinite(out).all())}
-                rows.append(row)
-        base = results[("classic", tpbs[0])]
-        for (name, tpb), (ups, out, res) in results.items():
+        runs = [(sw.ALG_CLASSIC, tpbs[0], 0)] + [(alg, tpb, th) for tpb in tpbs for th in thread_list
+                                                 for alg in (sw.ALG_SWEPT, sw.ALG_VARIANT)]
+        for alg, tpb, th in runs:
+            cfg = sw.make_config(prob, prec, alg=alg, nx=nx, tpb=tpb, dt=dt, bc=bc,
+                                 time_mode=sw.TIME_STEPS, n_steps=steps)
+            cfg.threads = th
+            ic = sw.initial_condition(cfg)
+            if prob == 2:
+                dev = np.zeros((nx, 4), dtype=ic.dtype)
+                dev[:, :3] = ic.reshape(-1, 3)
+                ic = dev.ravel()
+            elif prob == 0 and bc == 2:
+                x = np.arange(nx)
+                ic = (50 + 100 * np.sin(2 * np.pi * x / nx)).astype(ic.dtype)
+            st = torch.from_numpy(ic).cuda()
+            solver.run_device(cfg, st.data_ptr(), stream.cuda_stream)  # warm
+            st = torch.from_numpy(ic).cuda()
+            torch.cuda.synchronize()
+            res = solver.run_device(cfg, st.data_ptr(), stream.cuda_stream)
+            out = st.cpu().numpy()
+            ups = nx * steps / (res.kernel_ms * 1e-3)
+            key = ("classic" if alg == 0 else "swept" if alg == 1 else "variant", tpb, th)
+            results[key] = (ups, out, res)
+            row = {"case": label, "precision": prec, "alg": key[0], "tpb": tpb if alg else None,
+                   "threads": th if alg else None,
+                   "tile": res.tile, "nx": nx, "steps": steps, "ms": res.kernel_ms,
+                   "cell_updates_per_s": ups, "launches": res.launches,
+                   "finite": bool(np.isfinite(out).all())}
+            rows.append(row)
+        base = results[("classic", tpbs[0], 0)]
+        for (name, tpb, th), (ups, out, res) in results.items():
             same = np.array_equal(out, base[1])
             for r in rows:
                 if r["case"] == label and r["precision"] == prec and r["alg"] == name and \
-                        (r["tpb"] == tpb or name == "classic"):
+                        (name == "classic" or (r["tpb"] == tpb and r["threads"] == th)):
                     r["equal_to_classic"] = bool(same)
                     r["over_classic"] = ups / base[0]
         for r in rows:
             if r["case"] == label and r["precision"] == prec:
-                print("%-34s f%-2d %-8s tpb=%-5s %10.3e cell-updates/s  x%.2f vs classic  %s" % (
-                    label, prec * 8, r["alg"], r["tpb"], r["cell_updates_per_s"], r.get("over_classic", 1.0),
+                print("%-34s f%-2d %-8s tpb=%-5s thr=%-4s %10.3e cell-updates/s  x%.2f vs classic  %s" % (
+                    label, prec * 8, r["alg"], r["tpb"], r["threads"] or "-", r["cell_updates_per_s"],
+                    r.get("over_classic", 1.0),
                     "bit-identical" if r.get("equal_to_classic") else "DIFFERS"), flush=True)
     if args.ensemble:
         rows += ensemble_rows(sw, solver, args.quick)

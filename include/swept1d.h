@@ -79,7 +79,7 @@ typedef struct sw_config {
     int32_t alg;         /* enum sw_alg */
     int32_t bc;          /* enum sw_bc */
     int64_t nx;          /* spatial points (argv[1]) */
-    int32_t tpb;         /* points per swept node = threads per block (argv[2]) */
+    int32_t tpb;         /* points per swept node (argv[2]; the reference runs a thread per point) */
     int32_t time_mode;   /* enum sw_time_mode */
     double dt;           /* time step (argv[3]) */
     double tf;           /* finish time as given (argv[4]); the library applies tf - dt/4 like main() */
@@ -91,7 +91,8 @@ typedef struct sw_config {
     double gamma;        /* Euler heat-capacity ratio 1.4 */
     double left[3];      /* Euler left state (rho, u, p); all 0 = Sod (1, 0, 1) */
     double right[3];     /* Euler right state (rho, u, p); all 0 = Sod (0.125, 0, 0.1) */
-    int32_t threads;     /* ensembles: threads per swept block (0 = one per cell, capped at the kernel's limit) */
+    int32_t threads;     /* threads per swept block: 0 = the library's default for the tile width; a
+                            multiple of 32 up to min(tpb, 512) (Euler 256), else the default */
     int32_t reserved;
 } sw_config;
 

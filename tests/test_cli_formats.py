@@ -81,3 +81,36 @@ def test_perform_parser(sw, tmp_path):
     assert p.headers == ["Num Spatial Points", "Threads per Block", "Time per timestep (us)"]
     assert p.dataMatrix[1024][128] == 2.5
     assert p.best()[1024] == (2.5, 128)
+
+
+@pytest.mark.parametrize("prog,pid,prec", [("KSDoubleOut", 1, 8), ("HeatSingleOut", 0, 4), ("EulerDoubleOut", 2, 8)])
+def test_npy_header_and_initial_rows(sw, oracle, bins, tmp_path, prog, pid, prec):
+    """A .npy solution path: the header record and the initial-condition rows
+    are written before any device work, so they are checked here with or
+    without a GPU (the run itself then fails on a machine without one)."""
+    out = tmp_path / "sol.npy"
+    subprocess.run([str(bins[prog]), "512", "64", "1e-5", "1e-3", "1e-3", "1", str(out)], capture_output=True,
+                   text=True)
+    a = np.load(out)
+    assert a.dtype.names == ("var", "t", "v")
+    assert a["v"].dtype == (np.float64 if prec == 8 else np.float32)
+    head, rows = sw.formats.read_snapshots(out)
+    ic = oracle.reference_ic(pid, prec, 512)
+    n = 510 if pid == 2 else 512
+    assert int(head[1]) == n and a["v"].shape[1] == n
+    if pid == 2:
+        q = ic.reshape(-1, 3)[1:-1]
+        assert [r[0] for r in rows[:4]] == ["Density", "Velocity", "Energy", "Pressure"]
+        np.testing.assert_array_equal(rows[0][2], q[:, 0])
+        np.testing.assert_array_equal(rows[1][2], q[:, 1])          # the IC row holds rho*u, as in the .dat
+        np.testing.assert_array_equal(rows[2][2], q[:, 2] / q[:, 0])
+    else:
+        assert rows[0][0] == ("Temperature" if pid == 0 else "Velocity") and rows[0][1] == 0.0
+        np.testing.assert_array_equal(rows[0][2], ic)
+
+
+def test_snapshot_reader_rejects_other_arrays(sw, tmp_path):
+    f = tmp_path / "x.npy"
+    np.save(f, np.zeros(4))
+    with pytest.raises(ValueError):
+        sw.formats.read_snapshots(f)

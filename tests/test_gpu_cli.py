@@ -112,3 +112,37 @@ def test_ks_selftest(sw, tmp_path):
     r = _run(_bin(sw, "KSDoubleOut"), [1024, 64, 1e-5, 0.01, 1, 3, tmp_path / "k.dat"], ok=False)
     assert r.returncode == 255
     assert r.stdout.count("EQUAL!") == 3 and "NOT EQUAL" not in r.stdout, r.stdout
+
+
+@pytest.mark.parametrize("prec", ["Single", "Double"])
+@pytest.mark.parametrize("prob", ["Heat", "KS", "Euler"])
+def test_npy_rows_equal_dat_rows(sw, oracle, tmp_path, prob, prec):
+    """The .npy solution holds the .dat's rows: same names and times, and every
+    value printed at precision 10 is the .dat's token; the final row is the
+    oracle's classic state itself, unrounded."""
+    p = PID[prob]
+    nx, tpb = 512, 64
+    dt = {0: 0.004, 1: 0.005, 2: 0.1 / 510}[p]
+    q = tpb // (2 * oracle.RADIUS[p] * oracle.SUBSTEPS[p])
+    tf, freq = 24 * q * dt, 9 * q * dt
+    dat, npy = tmp_path / "s.dat", tmp_path / "s.npy"
+    args = [nx, tpb, repr(dt), repr(tf), repr(freq), 1]
+    _run(_bin(sw, prob + prec + "Out"), args + [dat])
+    _run(_bin(sw, prob + prec + "Out"), args + [npy])
+    hd, rd = sw.read_dat(dat)
+    hn, rn = sw.read_dat(npy)
+    assert int(hn[1]) == int(hd[1]) and len(rn) == len(rd)
+    assert abs(float(hn[0]) - float(hd[0])) <= 1e-9 * float(hd[0])
+    text_rows = [ln.split() for ln in dat.read_text().splitlines()[1:] if ln.strip()]
+    for (name_d, t_d, _), (name_n, t_n, v_n), tokens in zip(rd, rn, text_rows):
+        assert name_n == name_d
+        assert abs(t_n - t_d) <= 1e-9 * max(1.0, abs(t_d))
+        assert tokens[2:] == [_fmt(v) for v in v_n], (prob, prec, t_n)
+    bytes_ = 8 if prec == "Double" else 4
+    cfg = sw.make_config(p, bytes_, alg=1, nx=nx, tpb=tpb, dt=dt, tf=tf, freq=freq)
+    info, _, _ = sw.plan(cfg)
+    fin = oracle.classic(oracle.reference_consts(p, bytes_, nx, dt), oracle.reference_ic(p, bytes_, nx), info.n_steps)
+    if p == 2:
+        np.testing.assert_array_equal(rn[-4][2], fin.reshape(-1, 3)[1:-1, 0])
+    else:
+        np.testing.assert_array_equal(rn[-1][2], fin)

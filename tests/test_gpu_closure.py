@@ -123,3 +123,39 @@ def test_training_gains_over_plain_coarse_step(sw, solver, cl):
     c.step(learned, 25, use_closure=True)
     e_plain, e_learned = cl.rel_l2(plain, judge), cl.rel_l2(learned, judge)
     assert e_learned < 0.7 * e_plain, (e_learned, e_plain)
+
+
+def test_adaptive_fallback_and_selector(sw, solver, cl):
+    """run_adaptive: with tau = 0 every domain falls back, and the result is
+    the coarse-grained fine solution from the exact start, bit for bit; with
+    tau = inf none does, and every (domain, segment) runs closure or plain."""
+    fine0 = cl.fine_ensemble(6, seed=321)
+    c = cl.Closure(solver, seed=0)
+    u, info = cl.run_adaptive(solver, c, fine0, coarse_steps=20, segment=10, tau=0.0)
+    assert info["fallback"] == 6 and info["closure"] + info["plain"] == 0
+    f = fine0.clone()
+    cl.advance_fine(solver, f, 20 * cl.FACTOR)
+    assert torch.equal(u, cl.coarse_grain(solver, f))
+    u, info = cl.run_adaptive(solver, c, fine0, coarse_steps=20, segment=10, tau=float("inf"))
+    assert info["fallback"] == 0 and info["closure"] + info["plain"] == 12
+    assert bool(torch.isfinite(u).all())
+
+
+def test_adaptive_estimate_tracks_error(sw, solver, cl):
+    """On the smooth ensemble the plain coarse step is accurate: nothing falls
+    back, the accumulated estimate stays small, and the actual error does not
+    exceed the estimate by more than a small factor (the estimate sums the
+    residuals' norms, so cancellation can only make the error smaller)."""
+    fine0 = cl.fine_ensemble(8, seed=77)
+    c = cl.Closure(solver, seed=0)          # untrained: its correction is noise
+    steps = 100
+    u, info = cl.run_adaptive(solver, c, fine0, coarse_steps=steps, segment=25, tau=1.0)
+    assert info["fallback"] == 0
+    judge = fine0.clone()
+    cl.advance_fine(solver, judge, steps * cl.FACTOR)
+    ref = cl.coarse_grain(solver, judge)
+    err = (u.double() - ref.double()).norm(dim=1) / ref.double().norm(dim=1)
+    est = info["estimate"]
+    assert float(err.max()) < 1e-3, err
+    assert float(est.max()) < 1e-3, est
+    assert bool((err < 4 * est + 1e-6).all()), (err, est)

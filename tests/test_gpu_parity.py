@@ -95,6 +95,27 @@ def test_tile_widths(sw, solver, oracle, problem, tpb):
 
 
 @pytest.mark.parametrize("prec", [8, 4])
+@pytest.mark.parametrize("problem", [HEAT, KS, EULER])
+def test_threads_per_block(sw, solver, oracle, problem, prec):
+    """Any threads per swept block gives the same bits: 4 contiguous cells per
+    thread (tpb / 4), a strided walk (tpb / 2, 32), one per cell, and requests
+    out of range (33, 2 * tpb, 4096) that fall back to the default."""
+    nx, tpb = 2048, 256
+    dt = PROBLEM_DT[problem] if problem != EULER else 0.1 / (nx - 2)
+    c = _case(oracle, problem, prec, nx, dt)
+    ic = _ic(oracle, problem, prec, nx, kind="random", seed=17)
+    q = tpb // (2 * oracle.RADIUS[problem] * oracle.SUBSTEPS[problem])
+    nsteps = 3 * q + 1
+    want = oracle.classic(c, ic, nsteps)
+    for alg in (SWEPT, VARIANT):
+        for th in (0, 32, 64, 128, 256, 33, 512, 4096):
+            cfg = sw.make_config(problem, prec, alg=alg, nx=nx, tpb=tpb, dt=dt, time_mode=TIME_STEPS, n_steps=nsteps)
+            cfg.threads = th
+            got, _, _ = solver.run(cfg, ic)
+            _assert_identical(got, want, "problem %d prec %d alg %d threads %d" % (problem, prec, alg, th))
+
+
+@pytest.mark.parametrize("prec", [8, 4])
 def test_heat_periodic(sw, solver, oracle, prec):
     """Heat on a periodic domain (the benchmark's boundary), all paths."""
     nx, tpb, dt = 1024, 128, 0.004
