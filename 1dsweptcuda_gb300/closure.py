@@ -1,6 +1,6 @@
 """Learned closure for 4x-coarsened KS (the C ABI's sw_closure_* calls).
 
-Fine grid: nx = 4096, dx = 0.5, dt = 0.005, FP64 (the judge and the source of
+Fine grid: nx = 4096, dx = 0.5, dt = 0.005, FP64 (the reference solution and the source of
 training data).  Coarse grid: nx = 1024, dx = 2, dt = 0.02 = 4 fine steps,
 FP32.  The closure f learns the coarse step's defect
 
@@ -315,9 +315,9 @@ def evaluate(n_train: int = 512, snapshots: int = 64, n_eval: int = 1024, horizo
              start_step: int = 0) -> dict:
     """Train, then for each horizon tf solve the evaluation ensemble (n_eval
     domains, 4096 fine cells) from t0 = start_step * 0.02 to t0 + tf four
-    ways -- fine FP64 (the judge), plain coarse, closure-corrected coarse, and
+    ways -- fine FP64 (the reference solution), plain coarse, closure-corrected coarse, and
     run_adaptive with tolerance tau -- and report wall times and the relative
-    L2 error of each against the coarse-grained judge."""
+    L2 error of each against the coarse-grained reference solution."""
     torch = _torch()
     sw = _sw()
     solver = sw.Solver(0)
@@ -335,9 +335,9 @@ def evaluate(n_train: int = 512, snapshots: int = 64, n_eval: int = 1024, horizo
     run_adaptive(solver, closure, fine0, 2 * segment, segment, float("inf"))
     for tf in horizons:
         steps = int(round(tf / COARSE_DT))
-        judge = fine0.clone()
-        _, t_fine = _timed(lambda: advance_fine(solver, judge, steps * FACTOR))
-        ref = coarse_grain(solver, judge)
+        truth = fine0.clone()
+        _, t_fine = _timed(lambda: advance_fine(solver, truth, steps * FACTOR))
+        ref = coarse_grain(solver, truth)
         row = {"tf": tf, "time_fine_s": t_fine}
         for name, on in (("plain", False), ("closure", True)):
             v = start.clone()

@@ -1,5 +1,5 @@
 // C ABI of libswept1d: contexts, configuration, the reference's constants and
-// initial conditions, and the run driver that replaces classicWrapper /
+// initial conditions, and the run loop that replaces classicWrapper /
 // sweptWrapper of the reference programs.
 #include <cuda_runtime.h>
 

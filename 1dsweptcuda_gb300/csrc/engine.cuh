@@ -280,13 +280,65 @@ __device__ __forceinline__ void tile_span4(const Params<T> &p, T *rows, int L, i
         if (x0 + i >= lo && x0 + i < hi) dst[x0 + i] = o[i];
 }
 
+// Euler sub-step over tile cells [lo, hi) with every interface computed once.
+// A warp takes 29 cells at a time: lane l (cell b = s0 + l) loads cells
+// b-2..b+1, forms D(b-2, b-1) and the interface (b-1, b) -- taking D(b-1, b)
+// and D(b, b+1) from lanes l+1 and l+2 -- and adds its own interface minus the
+// one of lane l+1.  Lanes 29..31 only feed lanes below them; loop bounds are
+// warp-uniform so that every lane reaches every shuffle.  Values read past
+// W + R - 1 (clamped) only reach lanes whose cells are not stored.
+constexpr int kEulerCellsPerWarp = 29;
+
+template <typename T>
+__device__ __forceinline__ Q3<T> shfl_down3(Q3<T> v, int d) {
+    return q3(__shfl_down_sync(0xffffffffu, v.x, d), __shfl_down_sync(0xffffffffu, v.y, d),
+              __shfl_down_sync(0xffffffffu, v.z, d));
+}
+
+template <typename T>
+__device__ __forceinline__ void euler_level(const Params<T> &p, T *rows, int L, int W, int par, int lo, int hi, Ends e) {
+    constexpr int R = Scheme<SW_EULER, T>::R;
+    const T *src = rows + (par ^ 1) * 3 * L + R;
+    T *dst = rows + par * 3 * L + R;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    const T scale = par ? ml(T(0.25), p.dtdx) : ml(T(0.5), p.dtdx);
+    for (int s0 = lo + warp * kEulerCellsPerWarp; s0 < hi; s0 += nwarp * kEulerCellsPerWarp) {
+        const int b = s0 + lane;
+        Q3<T> c[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int x = min(b - 2 + k, W + R - 1);
+            c[k] = q3(src[x], src[L + x], src[2 * L + x]);
+        }
+        // zero across the domain's ends (the reference's edge flags, Euler1D_SweptShared.cu:311-335)
+        const T D = (b - 1 == e.first || b - 2 == e.last) ? T(0) : eu_pdiff(c[0], c[1]);
+        const T D1 = __shfl_down_sync(0xffffffffu, D, 1), D2 = __shfl_down_sync(0xffffffffu, D, 2);
+        Q3<T> F, S;
+        eu_iface(p, c[0], c[1], c[2], c[3], D, D1, D2, F, S);
+        const Q3<T> Fr = shfl_down3(F, 1), Sr = shfl_down3(S, 1);
+        if (lane < kEulerCellsPerWarp && b < hi && b != e.first && b != e.last) {
+            const Q3<T> base = par ? c[2] : q3(dst[b], dst[L + b], dst[2 * L + b]);
+            const Q3<T> o = qadd(base, qscale(scale, eu_combine(F, S, Fr, Sr)));
+            dst[b] = o.x;
+            dst[L + b] = o.y;
+            dst[2 * L + b] = o.z;
+        }
+    }
+}
+
 // Down part: sub-steps j = 1..H on the growing centre [W/2 - jR, W/2 + jR).
 template <int P, typename T>
 __device__ __forceinline__ void tile_down(const Params<T> &p, T *rows, int L, int W, int64_t base) {
     constexpr int R = Scheme<P, T>::R;
     const int h = W >> 1, H = W / (2 * R);
     const Ends e = tile_ends(base, p.nx, W, R);
-    if constexpr (P != SW_EULER) {
+    if constexpr (P == SW_EULER) {
+        for (int j = 1; j <= H; ++j) {
+            euler_level<T>(p, rows, L, W, j & 1, h - j * R, h + j * R, e);
+            __syncthreads();
+        }
+        return;
+    } else {
         if ((int)blockDim.x * 4 == W) {
             for (int j = 1; j <= H; ++j) {
                 tile_span4<P, T>(p, rows, L, j & 1, h - j * R, h + j * R, e);
@@ -295,9 +347,10 @@ __device__ __forceinline__ void tile_down(const Params<T> &p, T *rows, int L, in
             return;
         }
     }
+    // the live cells of each level start at the lowest thread: whole warps idle, not part-empty ones
     for (int j = 1; j <= H; ++j) {
-        for (int x = threadIdx.x; x < W; x += blockDim.x)
-            if (x >= h - j * R && x < h + j * R) tile_point<P, T>(p, rows, L, j & 1, x, e);
+        for (int x = h - j * R + (int)threadIdx.x; x < h + j * R; x += blockDim.x)
+            tile_point<P, T>(p, rows, L, j & 1, x, e);
         __syncthreads();
     }
 }
@@ -307,7 +360,13 @@ __device__ __forceinline__ void tile_up(const Params<T> &p, T *rows, int L, int 
     constexpr int R = Scheme<P, T>::R;
     const int H = W / (2 * R);
     const Ends e = tile_ends(base, p.nx, W, R);
-    if constexpr (P != SW_EULER) {
+    if constexpr (P == SW_EULER) {
+        for (int u = 1; u < H; ++u) {
+            euler_level<T>(p, rows, L, W, u & 1, u * R, W - u * R, e);
+            __syncthreads();
+        }
+        return;
+    } else {
         if ((int)blockDim.x * 4 == W) {
             for (int u = 1; u < H; ++u) {
                 tile_span4<P, T>(p, rows, L, u & 1, u * R, W - u * R, e);
@@ -317,8 +376,8 @@ __device__ __forceinline__ void tile_up(const Params<T> &p, T *rows, int L, int 
         }
     }
     for (int u = 1; u < H; ++u) {
-        for (int x = threadIdx.x; x < W; x += blockDim.x)
-            if (x >= u * R && x < W - u * R) tile_point<P, T>(p, rows, L, u & 1, x, e);
+        for (int x = u * R + (int)threadIdx.x; x < W - u * R; x += blockDim.x)
+            tile_point<P, T>(p, rows, L, u & 1, x, e);
         __syncthreads();
     }
 }
@@ -448,6 +507,45 @@ __global__ void __launch_bounds__(Scheme<P, T>::CMAXT) k_classic(const Params<T>
     if (g < p.nx) classic_cell<P, T>(p, in, out, sub, g);
 }
 
+// Classic Euler sub-step with shared interfaces (the warp scheme of
+// euler_level over the whole domain, 29 cells per warp).  Cells 0 and nx-1
+// hold the Dirichlet states (classicEuler, Euler1D_SweptShared.cu:400-426).
+template <typename T>
+__global__ void __launch_bounds__(256) k_classic_euler(const Params<T> p, const V4<T> *__restrict__ in,
+                                                       V4<T> *__restrict__ out, const int sub) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t b = warp * kEulerCellsPerWarp + lane, nx = p.nx;
+    Q3<T> c[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        int64_t q = b - 2 + k;
+        q = q < 0 ? 0 : (q >= nx ? nx - 1 : q);  // clamped values only reach cells that are not stored
+        const V4<T> v = in[q];
+        c[k] = q3(v.x, v.y, v.z);
+    }
+    const T D = (b - 1 == 0 || b - 2 == nx - 1) ? T(0) : eu_pdiff(c[0], c[1]);
+    const T D1 = __shfl_down_sync(0xffffffffu, D, 1), D2 = __shfl_down_sync(0xffffffffu, D, 2);
+    Q3<T> F, S;
+    eu_iface(p, c[0], c[1], c[2], c[3], D, D1, D2, F, S);
+    const Q3<T> Fr = shfl_down3(F, 1), Sr = shfl_down3(S, 1);
+    if (lane >= kEulerCellsPerWarp || b >= nx) return;
+    if (b == 0 || b == nx - 1) {
+        const int side = (b == 0) ? 0 : 1;
+        out[b] = V4<T>{p.bd[3 * side], p.bd[3 * side + 1], p.bd[3 * side + 2], T(0)};
+        return;
+    }
+    Q3<T> base = c[2];
+    T scale = ml(T(0.25), p.dtdx);
+    if (sub) {
+        const V4<T> u = out[b];
+        base = q3(u.x, u.y, u.z);
+        scale = ml(T(0.5), p.dtdx);
+    }
+    const Q3<T> o = qadd(base, qscale(scale, eu_combine(F, S, Fr, Sr)));
+    out[b] = V4<T>{o.x, o.y, o.z, T(0)};
+}
+
 // Euler host layout (rho, rho u, E) <-> device layout (rho, rho u, E, 0).
 template <typename T>
 __global__ void k_pack3(const T *__restrict__ in3, V4<T> *__restrict__ out4, int64_t nx) {
@@ -476,6 +574,12 @@ cudaError_t launch_classic(const void *vp, const void *in, void *out, int sub, i
                            cudaStream_t s) {
     using G = typename Scheme<P, T>::G;
     const Params<T> &p = *static_cast<const Params<T> *>(vp);
+    if constexpr (P == SW_EULER) {
+        const int64_t warps = (nx + kEulerCellsPerWarp - 1) / kEulerCellsPerWarp;
+        k_classic_euler<T><<<(unsigned)((warps + 7) / 8), 256, 0, s>>>(p, static_cast<const G *>(in),
+                                                                       static_cast<G *>(out), sub);
+        return cudaGetLastError();
+    }
     if (block <= 0 || block > Scheme<P, T>::CMAXT) block = block <= 0 ? 256 : Scheme<P, T>::CMAXT;
     const int64_t grid = (nx + block - 1) / block;
     k_classic<P, T><<<(unsigned)grid, block, 0, s>>>(p, static_cast<const G *>(in), static_cast<G *>(out), sub);

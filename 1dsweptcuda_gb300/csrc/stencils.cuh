@@ -152,6 +152,38 @@ __device__ __forceinline__ Q3<T> eu_flux_sum(const Params<T> &p, const Q3<T> (&s
     flux = qsub(flux, eu_spectral(p, tL, tR));
     return flux;
 }
+// Interface form of eu_flux_sum.  Each interface's terms are the same in the
+// two cells that share it, so one lane computes them once:
+//  * eu_pdiff(a, b): the pressure-difference numerator between neighbours a
+//    (left) and b (right).  The reference spells the product 2*b.x*a.x for a
+//    cell's left interfaces and 2*a.x*b.x for its right ones; the doubling is
+//    exact, so both round to the same value;
+//  * eu_iface: the limited states of the interface between a and b (outer
+//    neighbours am, bp; Da = D(am, a), Db = D(a, b), Dbp = D(b, bp)) and its
+//    flux F and dissipation S, as eulerStutterStep / eulerFinalStep form them
+//    (:336-341 for a cell's left interface, :375-380 for its right one);
+//  * eu_combine: the cell's sum ((F_left + S_left) - F_right) - S_right, in
+//    the reference's order.
+template <typename T>
+__device__ __forceinline__ T eu_pdiff(Q3<T> a, Q3<T> b) {
+    return ad(ml(ml(ml(T(2), b.x), a.x), sb(b.z, a.z)), sb(ml(ml(a.y, a.y), b.x), ml(ml(b.y, b.y), a.x)));
+}
+template <typename T>
+__device__ __forceinline__ void eu_iface(const Params<T> &p, Q3<T> am, Q3<T> a, Q3<T> b, Q3<T> bp, T Da, T Db, T Dbp,
+                                         Q3<T> &F, Q3<T> &S) {
+    const T Z = T(0);
+    const bool skipA = (Da == Z) || (Db == Z) || ((Da < Z) != (Db < Z));
+    const bool skipB = (Db == Z) || (Dbp == Z) || ((Db < Z) != (Dbp < Z));
+    const Q3<T> tL = skipA ? a : eu_limit(a, b, dv(ml(am.x, Db), ml(b.x, Da)));
+    const Q3<T> tR = skipB ? b : eu_limit(b, a, dv(ml(bp.x, Db), ml(a.x, Dbp)));
+    F = eu_flux(p, tL, tR);
+    S = eu_spectral(p, tL, tR);
+}
+template <typename T>
+__device__ __forceinline__ Q3<T> eu_combine(Q3<T> Fl, Q3<T> Sl, Q3<T> Fr, Q3<T> Sr) {
+    return qsub(qsub(qadd(Fl, Sl), Fr), Sr);
+}
+
 // eulerStutterStep result, :345: s2 + (0.25*dt_dx)*flux
 template <typename T>
 __device__ __forceinline__ Q3<T> eu_predict(const Params<T> &p, const Q3<T> (&s)[5], bool fl, bool fr) {

@@ -3,7 +3,7 @@ time classic, swept and variant over problems, precisions, nx and tpb with the
 state resident on the device, and check that all paths agree bit for bit.
 
     python 1dsweptcuda_gb300/perf.py [--quick] [--ensemble] [--only TEXT] [--precision 4|8]
-                                     [--threads 0,64,...] [--json out.json]
+                                     [--threads 0,64,...] [--tpb 256,...] [--algs swept,...] [--json out.json]
 
 Each case runs SW_TIME_STEPS with a step count that is a whole number of swept
 cycles for every tpb in the case, timed with CUDA events inside the library
@@ -88,19 +88,26 @@ def main():
     ap.add_argument("--only", default=None, help="run only cases whose label contains one of these comma-separated texts")
     ap.add_argument("--precision", type=int, default=None, choices=[4, 8], help="run only this precision")
     ap.add_argument("--threads", default="0", help="comma-separated threads per swept block (0 = default)")
+    ap.add_argument("--tpb", default=None, help="comma-separated tile widths (default: each case's own)")
+    ap.add_argument("--algs", default="classic,swept,variant", help="comma-separated subset of classic,swept,variant")
     args = ap.parse_args()
     sw = importlib.import_module("1dsweptcuda_gb300")
     solver = sw.Solver(0)
     stream = torch.cuda.current_stream()
     thread_list = [int(t) for t in args.threads.split(",")]
+    algs = {"classic": sw.ALG_CLASSIC, "swept": sw.ALG_SWEPT, "variant": sw.ALG_VARIANT}
+    alg_list = [algs[a] for a in args.algs.split(",")]
     rows = []
     for label, prob, prec, bc, nx, tpbs, steps, dt in cases(args.quick):
         if (args.only and not any(o in label for o in args.only.split(","))) or \
                 (args.precision and args.precision != prec):
             continue
         results = {}
-        runs = [(sw.ALG_CLASSIC, tpbs[0], 0)] + [(alg, tpb, th) for tpb in tpbs for th in thread_list
-                                                 for alg in (sw.ALG_SWEPT, sw.ALG_VARIANT)]
+        if args.tpb:
+            tpbs = [int(t) for t in args.tpb.split(",")]
+        runs = [(sw.ALG_CLASSIC, tpbs[0], 0)] if sw.ALG_CLASSIC in alg_list else []
+        runs += [(alg, tpb, th) for tpb in tpbs for th in thread_list for alg in (sw.ALG_SWEPT, sw.ALG_VARIANT)
+                 if alg in alg_list]
         for alg, tpb, th in runs:
             cfg = sw.make_config(prob, prec, alg=alg, nx=nx, tpb=tpb, dt=dt, bc=bc,
                                  time_mode=sw.TIME_STEPS, n_steps=steps)
@@ -128,7 +135,7 @@ def main():
                    "cell_updates_per_s": ups, "launches": res.launches,
                    "finite": bool(np.isfinite(out).all())}
             rows.append(row)
-        base = results[("classic", tpbs[0], 0)]
+        base = results.get(("classic", tpbs[0], 0)) or next(iter(results.values()))
         for (name, tpb, th), (ups, out, res) in results.items():
             same = np.array_equal(out, base[1])
             for r in rows:
@@ -141,7 +148,8 @@ def main():
                 print("%-34s f%-2d %-8s tpb=%-5s thr=%-4s %10.3e cell-updates/s  x%.2f vs classic  %s" % (
                     label, prec * 8, r["alg"], r["tpb"], r["threads"] or "-", r["cell_updates_per_s"],
                     r.get("over_classic", 1.0),
-                    "bit-identical" if r.get("equal_to_classic") else "DIFFERS"), flush=True)
+                    ("bit-identical" if r.get("equal_to_classic") else "DIFFERS") if sw.ALG_CLASSIC in alg_list
+                    else ""), flush=True)
     if args.ensemble:
         rows += ensemble_rows(sw, solver, args.quick)
     solver.close()

@@ -41,12 +41,15 @@ TF = 200.0
 NSTEPS = 40000            # tf / dt
 B_CLASSIC_KS_F64 = 40     # algorithmic bytes per cell-update of the classic KS FP64 scheme
 DP_OPS_PER_UPDATE = 30    # FP64 instructions per cell-update: 2 sub-steps x 15 (exact power-of-two folds)
-# FP64 pipe issue rate of this GB300 pool, measured with a DFMA throughput
-# probe: 0.600e12 DFMA/s (2.06 per clock per SM at 1.92 GHz; 1.2 TFLOP/s).
-FP64_OPS_PEAK = 0.600e12
-BASELINE_K40_KS_F64_SWEPT = 1.07e10  # KS FP64 swept, nx=2^20, K40c
+# FP64 pipe issue rates of this GB300 pool, measured with a throughput probe
+# (152 SMs at 2.07 GHz): DFMA 0.627e12/s (1.99 per clock per SM, 1.25 TFLOP/s),
+# DADD and DMUL 0.528e12/s.  A KS sub-step is 5 FMA + 5 MUL + 5 ADD, so its
+# mix issues at 15 / (5 / 0.627 + 10 / 0.528) = 0.557e12 operations/s.
+FP64_OPS_PEAK = 0.627e12
+FP64_KS_MIX_PEAK = 15.0 / (5.0 / 0.627e12 + 10.0 / 0.528e12)
+K40_KS_F64_SWEPT_PUBLISHED = 1.07e10  # the reference's published KS FP64 swept figure, nx=2^20, on a K40c
 # DRAM bytes (read + write) of one diamond launch of this workload from one ncu
-# capture (profiles/ks_f64_swept_diamond_nx2e20.md; cold-cache replay).
+# capture of this launch (cold-cache replay).
 DIAMOND_TRAFFIC_BYTES = 16798720
 
 
@@ -283,21 +286,22 @@ def run_ours(args) -> None:
                     "diamond launch; the swept kernel's real DRAM traffic is far lower, its bound is the FP64 pipe"}
     dp = NX * steps_per_launch * DP_OPS_PER_UPDATE / (launch_ms * 1e-3)
     roof["fp64_pipe"] = {"achieved": dp / 1e12, "unit": "Tops/s", "ops_per_cell_update": DP_OPS_PER_UPDATE,
-                         "peak": FP64_OPS_PEAK / 1e12 if FP64_OPS_PEAK else None,
-                         "frac": dp / FP64_OPS_PEAK if FP64_OPS_PEAK else None}
+                         "peak": FP64_OPS_PEAK / 1e12, "frac": dp / FP64_OPS_PEAK,
+                         "ks_mix_peak": FP64_KS_MIX_PEAK / 1e12, "frac_of_ks_mix": dp / FP64_KS_MIX_PEAK,
+                         "peak_source": "measured (FP64 throughput probe on this GB300 pool)"}
 
     base = cpu_baseline(seconds=10.0) if world == 1 else None
     line = {
         "metric": "cell-updates/s (KS1D FP64 swept, nx=2^20, tpb=256, dt=0.005, tf=200)",
         "value": value, "unit": "cell-updates/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": value / BASELINE_K40_KS_F64_SWEPT, "dtype": "f64",
+        "vs_baseline": value / K40_KS_F64_SWEPT_PUBLISHED, "dtype": "f64",
         "data": "synthetic: the reference KS IC u(x,0) = 2cos(19 pi x/128)",
         "config": {"workload": "KS1D FP64 swept (alg 1), periodic, nx=2^20, tpb=256, dx=0.5, dt=0.005, tf=200 "
                                "(40000 time steps per step), state resident in HBM",
                    "nx": NX, "tpb": TPB, "time_steps_per_step": NSTEPS, "alg": "swept",
                    "l2": "flushed between steps (256 MiB write), outside the step timing",
-                   "vs_baseline_source": "BASELINE.md KS FP64 swept nx=2^20 on K40c, 1.07e10 cell-updates/s"},
+                   "vs_baseline_source": "the reference's published KS FP64 swept figure, nx=2^20, K40c: 1.07e10 cell-updates/s"},
         "e2e": {"value": e2e_value, "unit": "cell-updates/s", "h2d_bytes_per_step": NX * 8,
                 "d2h_bytes_per_step": NX * 8, "api": "sw_run (host IC -> host final state)"},
         "roofline": roof,

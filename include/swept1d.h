@@ -44,7 +44,7 @@ enum sw_status {
     SW_ERR_NOMEM = -5,       /* device or pinned host allocation failed */
     SW_ERR_IO = -6,          /* output file could not be opened or written */
     SW_ERR_TIMEOUT = -7,     /* a bounded inter-block wait expired; state not valid */
-    SW_ERR_UNSUPPORTED = -8, /* valid request this build does not provide */
+    SW_ERR_UNSUPPORTED = -8, /* valid request this library does not provide */
     SW_ERR_CALLBACK = -9,    /* the snapshot callback asked to stop */
     SW_ERR_USAGE = -10       /* too few command-line arguments (argc < 8) */
 };

@@ -1,7 +1,7 @@
 """CPU oracle for the swept 1D solvers -- TEST INFRASTRUCTURE ONLY.
 
 Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU legs of ``bench.py``
-import this package.  It is the checker: the product path (the CUDA library in
+import this package, to check results.  The product path (the CUDA library in
 ``1dsweptcuda_gb300``) never imports or calls it.
 
 ``liboracle.so`` (``oracle.c``) restates the reference's classic schemes in its

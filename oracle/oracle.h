@@ -1,8 +1,8 @@
 /*
  * CPU oracle for the swept-rule 1D stencil solvers -- TEST INFRASTRUCTURE ONLY.
  *
- * This library is the checker.  Only tests/, __graft_entry__.smoke() and the
- * cpu_baseline / reference legs of bench.py load it.  The product path (the
+ * Only tests/, __graft_entry__.smoke() and the cpu_baseline / reference legs of
+ * bench.py load this library, to check results and to time the CPU baseline.  The product path (the
  * CUDA library under 1dsweptcuda_gb300/) never links, loads or calls it.
  *
  * It restates, in plain C, the arithmetic of the reference programs

@@ -117,11 +117,11 @@ def test_training_gains_over_plain_coarse_step(sw, solver, cl):
     cl.advance_fine(solver, fine, spin * cl.FACTOR)
     start = cl.coarse_grain(solver, fine)
     cl.advance_fine(solver, fine, 25 * cl.FACTOR)
-    judge = cl.coarse_grain(solver, fine)
+    truth = cl.coarse_grain(solver, fine)
     plain, learned = start.clone(), start.clone()
     c.step(plain, 25, use_closure=False)
     c.step(learned, 25, use_closure=True)
-    e_plain, e_learned = cl.rel_l2(plain, judge), cl.rel_l2(learned, judge)
+    e_plain, e_learned = cl.rel_l2(plain, truth), cl.rel_l2(learned, truth)
     assert e_learned < 0.7 * e_plain, (e_learned, e_plain)
 
 
@@ -151,9 +151,9 @@ def test_adaptive_estimate_tracks_error(sw, solver, cl):
     steps = 100
     u, info = cl.run_adaptive(solver, c, fine0, coarse_steps=steps, segment=25, tau=1.0)
     assert info["fallback"] == 0
-    judge = fine0.clone()
-    cl.advance_fine(solver, judge, steps * cl.FACTOR)
-    ref = cl.coarse_grain(solver, judge)
+    truth = fine0.clone()
+    cl.advance_fine(solver, truth, steps * cl.FACTOR)
+    ref = cl.coarse_grain(solver, truth)
     err = (u.double() - ref.double()).norm(dim=1) / ref.double().norm(dim=1)
     est = info["estimate"]
     assert float(err.max()) < 1e-3, err
