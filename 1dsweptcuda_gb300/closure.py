@@ -360,6 +360,26 @@ def evaluate(n_train: int = 512, snapshots: int = 64, n_eval: int = 1024, horizo
     return out
 
 
+def bench_step(n_dom: int = 1024, steps: int = 200, seed: int = 0) -> dict:
+    """Throughput of the fused coarse step with the closure on (k_step), on
+    n_dom domains of the coarse grid from a smooth random state: coarse
+    cell-steps per second and the tensor-core work it implies (the 32 -> 32
+    layer is 2 * 32 * 32 * 5 FLOP per cell)."""
+    sw = _sw()
+    solver = sw.Solver(0)
+    closure = Closure(solver, seed=seed)
+    fine = fine_ensemble(n_dom, seed=seed + 1)
+    u = coarse_grain(solver, fine)
+    closure.step(u.clone(), 2, use_closure=True)          # warm-up
+    v = u.clone()
+    res = closure.step(v, steps, use_closure=True)
+    cells = n_dom * COARSE_NX * steps
+    out = {"n_dom": n_dom, "steps": steps, "ms": res.kernel_ms, "cell_steps_per_s": cells / (res.kernel_ms * 1e-3),
+           "layer2_tflops": cells * 2 * 32 * 32 * 5 / (res.kernel_ms * 1e-3) / 1e12}
+    solver.close()
+    return out
+
+
 if __name__ == "__main__":
     import argparse
     import json
@@ -376,7 +396,11 @@ if __name__ == "__main__":
     ap.add_argument("--segment", type=int, default=50)
     ap.add_argument("--start-step", type=int, default=0, help="coarse steps of spin-up before t0")
     ap.add_argument("--json", default=None)
+    ap.add_argument("--bench-step", type=int, default=0, help="only time this many fused closure steps")
     a = ap.parse_args()
+    if a.bench_step:
+        print(json.dumps(bench_step(steps=a.bench_step)))
+        sys.exit(0)
     res = evaluate(a.train_traj, a.snapshots, a.eval, [float(t) for t in a.horizons.split(",")], a.train_steps,
                    tau=a.tau, segment=a.segment, start_step=a.start_step)
     print(json.dumps(res, indent=1))

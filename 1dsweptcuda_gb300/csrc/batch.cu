@@ -54,7 +54,14 @@ int ensure_tables(sw_ctx *ctx, int32_t n, const int64_t *nx, int W) {
         tiles += nt;
     }
     off[n] = cells;
-    const size_t bytes = sizeof(int64_t) * (size_t)(2 * n + 1) + sizeof(int32_t) * dom.size() + 16;
+    // first domain of each classic block (empty domains are skipped by the kernel's forward walk)
+    std::vector<int32_t> blk((size_t)((cells + sw::kClassicBlock - 1) / sw::kClassicBlock));
+    for (int32_t d = 0, k = 0; k < (int32_t)blk.size(); ++k) {
+        const int64_t first = (int64_t)k * sw::kClassicBlock;
+        while (d + 1 < n && off[d + 1] <= first) ++d;
+        blk[k] = d;
+    }
+    const size_t bytes = sizeof(int64_t) * (size_t)(2 * n + 1) + sizeof(int32_t) * (dom.size() + blk.size()) + 16;
     SW_CUDA(ctx, sw::grow_dev(&bt.d_tables, &bt.n_tables, bytes));
     char *base = static_cast<char *>(bt.d_tables);
     int64_t *d_off = reinterpret_cast<int64_t *>(base);
@@ -63,7 +70,9 @@ int ensure_tables(sw_ctx *ctx, int32_t n, const int64_t *nx, int W) {
     SW_CUDA(ctx, cudaMemcpy(d_off, off.data(), sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice));
     SW_CUDA(ctx, cudaMemcpy(d_tile0, tile0.data(), sizeof(int64_t) * n, cudaMemcpyHostToDevice));
     if (!dom.empty()) SW_CUDA(ctx, cudaMemcpy(d_dom, dom.data(), sizeof(int32_t) * dom.size(), cudaMemcpyHostToDevice));
-    bt.dev = BatchDev{d_dom, d_off, d_tile0, tiles, cells, n};
+    int32_t *d_blk = d_dom + dom.size();
+    if (!blk.empty()) SW_CUDA(ctx, cudaMemcpy(d_blk, blk.data(), sizeof(int32_t) * blk.size(), cudaMemcpyHostToDevice));
+    bt.dev = BatchDev{d_dom, d_off, d_tile0, d_blk, tiles, cells, n};
     bt.nx.assign(nx, nx + n);
     bt.W = W;
     if (ctx->graph.exec) {  // the tables moved: a cached graph may point at the old ones

@@ -19,6 +19,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstddef>
 #include <cstdint>
 #include <cstring>
 #include <vector>
@@ -64,25 +65,42 @@ __device__ __forceinline__ void mma_bf16(float (&d)[4], uint32_t a0, uint32_t a1
         : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
 }
 
+// Shared memory of a tile.  The forward kernels allocate only the part up to
+// z2 (smem_fwd_bytes); the backward kernel also keeps the pre-activations.
 struct Smem {
     float us[NU];
     float w1[CH * KW], b1[CH], b2[CH], w3[CH * KW], b3, scale;
-    __nv_bfloat16 a1[NA1 * LDB];            // layer-1 activations, BF16 (the MMA A operand)
-    __nv_bfloat16 w2[KW * CH * LDB];        // w2[t][o][i], i contiguous (the MMA B operand)
-    float z2[NA2 * LDF];                    // layer-2 pre-activations
-    float a2[NA2 * LDF];                    // layer-2 activations gelu(z2)
-    float z1[NA1 * LDF];                    // layer-1 pre-activations (backward only)
+    __nv_bfloat16 a1[NA1 * LDB];                   // layer-1 activations, BF16 (the MMA A operand)
+    alignas(16) __nv_bfloat16 w2[KW * CH * LDB];   // w2[t][o][i], i contiguous (the MMA B operand)
+    float a2[NA2 * LDF];                           // layer-2 activations gelu(z2)
+    float pred[TOUT + 4];                          // k_step: the KS predictor on x0-2 .. x0+TOUT+1
+    float z2[NA2 * LDF];                           // layer-2 pre-activations (backward only)
+    float z1[NA1 * LDF];                           // layer-1 pre-activations (backward only)
 };
+constexpr int W2P_WORDS = KW * CH * LDB * 2 / 16;  // the staged w2 in 16-byte words
 
-// Load the tile's inputs (periodic within the domain) and the weights.
+// theta's w2 (flat [o][i][t], FP32) -> BF16 in the shared-memory layout [t][o][i]
+// (row stride LDB; the padding columns are zero), once per call of the
+// forward kernels instead of once per block.
+__global__ void k_pack_w2(const float *__restrict__ theta, __nv_bfloat16 *__restrict__ w2p) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= KW * CH * LDB) return;
+    const int t = k / (CH * LDB), o = (k / LDB) % CH, i = k % LDB;
+    w2p[k] = __float2bfloat16_rn(i < CH ? theta[OW2 + (o * CH + i) * KW + t] : 0.0f);
+}
+
+// Load the tile's inputs (periodic within the domain) and, unless `weights`
+// is false, the weights; w2 from the staged copy w2p (16-byte words) when
+// given, else from theta.
 __device__ void load_tile(Smem &s, const float *__restrict__ theta, const float *__restrict__ u, int64_t n,
-                          int64_t x0) {
+                          int64_t x0, const uint4 *__restrict__ w2p = nullptr, bool weights = true) {
     for (int j = threadIdx.x; j < NU; j += blockDim.x) {
         int64_t q = x0 - 6 + j;
         q %= n;
         if (q < 0) q += n;
         s.us[j] = u[q];
     }
+    if (!weights) return;
     for (int i = threadIdx.x; i < CH * KW; i += blockDim.x) {
         s.w1[i] = bf16r(theta[OW1 + i]);
         s.w3[i] = bf16r(theta[OW3 + i]);
@@ -95,6 +113,11 @@ __device__ void load_tile(Smem &s, const float *__restrict__ theta, const float 
         s.b3 = theta[OB3];
         s.scale = theta[OSCALE];
     }
+    if (w2p) {
+        uint4 *dst = reinterpret_cast<uint4 *>(s.w2);
+        for (int k = threadIdx.x; k < W2P_WORDS; k += blockDim.x) dst[k] = w2p[k];
+        return;
+    }
     // w2 flat is [o][i][t]; smem is [t][o][i]
     for (int k = threadIdx.x; k < CH * CH * KW; k += blockDim.x) {
         const int o = k / (CH * KW), i = (k / KW) % CH, t = k % KW;
@@ -102,15 +125,16 @@ __device__ void load_tile(Smem &s, const float *__restrict__ theta, const float 
     }
 }
 
-// Layers 1 and 2 of the forward pass: a1 (BF16), z2 and a2 = gelu(z2) (FP32).
-// Requires load_tile and a barrier first.
-__device__ void forward_12(Smem &s, bool keep_z1) {
+// Layers 1 and 2 of the forward pass: a1 (BF16) and a2 = gelu(z2) (FP32); with
+// TRAIN also the pre-activations z1 and z2.  Requires load_tile and a barrier first.
+template <bool TRAIN>
+__device__ void forward_12(Smem &s) {
     for (int k = threadIdx.x; k < NA1 * CH; k += blockDim.x) {
         const int r = k / CH, o = k % CH;
         float z = s.b1[o];
 #pragma unroll
         for (int t = 0; t < KW; ++t) z = fmaf(s.w1[o * KW + t], s.us[r + t], z);
-        if (keep_z1) s.z1[r * LDF + o] = z;
+        if (TRAIN) s.z1[r * LDF + o] = z;
         s.a1[r * LDB + o] = __float2bfloat16_rn(gelu(z));
     }
     __syncthreads();
@@ -141,15 +165,19 @@ __device__ void forward_12(Smem &s, bool keep_z1) {
             const int r0 = p0 + g, r1 = p0 + g + 8;
             if (r0 < NA2) {
                 const float z0 = acc[nt][0] + s.b2[o], z1 = acc[nt][1] + s.b2[o + 1];
-                s.z2[r0 * LDF + o] = z0;
-                s.z2[r0 * LDF + o + 1] = z1;
+                if (TRAIN) {
+                    s.z2[r0 * LDF + o] = z0;
+                    s.z2[r0 * LDF + o + 1] = z1;
+                }
                 s.a2[r0 * LDF + o] = gelu(z0);
                 s.a2[r0 * LDF + o + 1] = gelu(z1);
             }
             if (r1 < NA2) {
                 const float z2 = acc[nt][2] + s.b2[o], z3 = acc[nt][3] + s.b2[o + 1];
-                s.z2[r1 * LDF + o] = z2;
-                s.z2[r1 * LDF + o + 1] = z3;
+                if (TRAIN) {
+                    s.z2[r1 * LDF + o] = z2;
+                    s.z2[r1 * LDF + o + 1] = z3;
+                }
                 s.a2[r1 * LDF + o] = gelu(z2);
                 s.a2[r1 * LDF + o + 1] = gelu(z3);
             }
@@ -170,39 +198,40 @@ __device__ __forceinline__ float layer3(const Smem &s, int q) {
 
 // ---------------------------------------------------------------- kernels
 // delta = f(u) for every cell of n_dom domains of n cells (n a multiple of TOUT).
-__global__ void __launch_bounds__(THREADS) k_infer(const float *__restrict__ theta, const float *__restrict__ u,
-                                                   float *__restrict__ delta, int64_t n, int64_t tiles_per_dom) {
+__global__ void __launch_bounds__(THREADS) k_infer(const float *__restrict__ theta, const uint4 *__restrict__ w2p,
+                                                   const float *__restrict__ u, float *__restrict__ delta, int64_t n,
+                                                   int64_t tiles_per_dom) {
     extern __shared__ __align__(16) unsigned char raw[];
     Smem &s = *reinterpret_cast<Smem *>(raw);
     const int64_t dom = blockIdx.x / tiles_per_dom, x0 = (blockIdx.x % tiles_per_dom) * TOUT;
     const float *ud = u + dom * n;
-    load_tile(s, theta, ud, n, x0);
+    load_tile(s, theta, ud, n, x0, w2p);
     __syncthreads();
-    forward_12(s, false);
+    forward_12<false>(s);
     for (int q = threadIdx.x; q < TOUT; q += blockDim.x) delta[dom * n + x0 + q] = s.scale * layer3(s, q);
 }
 
 // One coarse KS step fused with the closure: u_out = classic KS step(u_in) + f(u_in).
 // The KS predictor/corrector reads u_in on [x0-4, x0+TOUT+4) from the same tile.
-__global__ void __launch_bounds__(THREADS) k_step(const float *__restrict__ theta, const Params<float> pk,
-                                                  const float *__restrict__ u, float *__restrict__ out, int64_t n,
-                                                  int64_t tiles_per_dom, int use_closure) {
+__global__ void __launch_bounds__(THREADS) k_step(const float *__restrict__ theta, const uint4 *__restrict__ w2p,
+                                                  const Params<float> pk, const float *__restrict__ u,
+                                                  float *__restrict__ out, int64_t n, int64_t tiles_per_dom,
+                                                  int use_closure) {
     extern __shared__ __align__(16) unsigned char raw[];
     Smem &s = *reinterpret_cast<Smem *>(raw);
     const int64_t dom = blockIdx.x / tiles_per_dom, x0 = (blockIdx.x % tiles_per_dom) * TOUT;
-    load_tile(s, theta, u + dom * n, n, x0);
+    load_tile(s, theta, u + dom * n, n, x0, w2p, use_closure != 0);  // theta may be null without the closure
     __syncthreads();
-    if (use_closure) forward_12(s, false);
-    // predictor on positions x0-2 .. x0+TOUT+1 (us index 4 .. TOUT+7), kept in z1 scratch (column 0)
+    if (use_closure) forward_12<false>(s);
+    // predictor on positions x0-2 .. x0+TOUT+1 (us index 4 .. TOUT+7)
     for (int j = threadIdx.x; j < TOUT + 4; j += blockDim.x) {
         const int c = j + 4;
-        s.z1[j * LDF] = ks_predict(pk, s.us[c - 2], s.us[c - 1], s.us[c], s.us[c + 1], s.us[c + 2]);
+        s.pred[j] = ks_predict(pk, s.us[c - 2], s.us[c - 1], s.us[c], s.us[c + 1], s.us[c + 2]);
     }
     __syncthreads();
     for (int q = threadIdx.x; q < TOUT; q += blockDim.x) {
         const int c = q + 6, j = q + 2;  // us index of x0+q; predictor index of x0+q
-        float v = ks_correct(pk, s.us[c], s.z1[(j - 2) * LDF], s.z1[(j - 1) * LDF], s.z1[j * LDF],
-                             s.z1[(j + 1) * LDF], s.z1[(j + 2) * LDF]);
+        float v = ks_correct(pk, s.us[c], s.pred[j - 2], s.pred[j - 1], s.pred[j], s.pred[j + 1], s.pred[j + 2]);
         if (use_closure) v += s.scale * layer3(s, q);
         out[dom * n + x0 + q] = v;
     }
@@ -234,7 +263,7 @@ __global__ void __launch_bounds__(THREADS) k_grad(const float *__restrict__ thet
         const int64_t dom = rows ? rows[b] : b;  // minibatch row -> sample
         load_tile(s, theta, u + dom * n, n, x0);
         __syncthreads();
-        forward_12(s, true);
+        forward_12<true>(s);
         // delta, dL/ddelta, loss, dW3, db3
         for (int q = threadIdx.x; q < TOUT; q += blockDim.x) {
             const float d = layer3(s, q);
@@ -401,6 +430,7 @@ __global__ void k_coarse_grain(const double *__restrict__ fine, float *__restric
 }
 
 constexpr size_t smem_bytes() { return sizeof(Smem); }
+constexpr size_t smem_fwd_bytes() { return offsetof(Smem, z2); }
 
 }  // namespace cl
 }  // namespace sw
@@ -417,13 +447,24 @@ int closure_check(sw_ctx *ctx, int32_t n_dom, int64_t n) {
 cudaError_t allow_smem() {
     static bool done = false;
     if (done) return cudaSuccess;
-    cudaError_t e = cudaFuncSetAttribute(cl::k_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cl::smem_bytes());
+    cudaError_t e =
+        cudaFuncSetAttribute(cl::k_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cl::smem_fwd_bytes());
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(cl::k_step, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cl::smem_bytes());
+        e = cudaFuncSetAttribute(cl::k_step, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cl::smem_fwd_bytes());
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(cl::k_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cl::smem_bytes());
     done = (e == cudaSuccess);
     return e;
+}
+
+// Stage theta's layer-2 weights for the forward kernels (stream-ordered before them).
+int stage_w2(sw_ctx *ctx, const float *theta, const uint4 **w2p) {
+    if (!ctx->d_w2p) SW_CUDA(ctx, cudaMalloc(&ctx->d_w2p, (size_t)cl::W2P_WORDS * 16));
+    const int total = cl::KW * cl::CH * cl::LDB;
+    cl::k_pack_w2<<<(total + 255) / 256, 256, 0, ctx->stream>>>(theta, static_cast<__nv_bfloat16 *>(ctx->d_w2p));
+    SW_CUDA(ctx, cudaGetLastError());
+    *w2p = static_cast<const uint4 *>(ctx->d_w2p);
+    return SW_OK;
 }
 
 }  // namespace
@@ -437,7 +478,11 @@ int sw_closure_infer(sw_ctx *ctx, const float *theta, const float *u, float *del
     SW_CUDA(ctx, cudaSetDevice(ctx->device));
     SW_CUDA(ctx, allow_smem());
     const int64_t tiles = n / cl::TOUT;
-    cl::k_infer<<<(unsigned)(tiles * n_dom), cl::THREADS, cl::smem_bytes(), ctx->stream>>>(theta, u, delta, n, tiles);
+    const uint4 *w2p = nullptr;
+    rc = stage_w2(ctx, theta, &w2p);
+    if (rc) return rc;
+    cl::k_infer<<<(unsigned)(tiles * n_dom), cl::THREADS, cl::smem_fwd_bytes(), ctx->stream>>>(theta, w2p, u, delta, n,
+                                                                                                tiles);
     SW_CUDA(ctx, cudaGetLastError());
     SW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return SW_OK;
@@ -460,9 +505,14 @@ int sw_closure_step(sw_ctx *ctx, const sw_config *coarse, const float *theta, fl
     float *alt = static_cast<float *>(ctx->d_work), *cur = u;
     const int64_t tiles = n / cl::TOUT;
     SW_CUDA(ctx, cudaEventRecord(ctx->k0, ctx->stream));
+    const uint4 *w2p = nullptr;
+    if (use_closure) {
+        rc = stage_w2(ctx, theta, &w2p);
+        if (rc) return rc;
+    }
     for (int64_t i = 0; i < n_steps; ++i) {
-        cl::k_step<<<(unsigned)(tiles * n_dom), cl::THREADS, cl::smem_bytes(), ctx->stream>>>(theta, p, cur, alt, n,
-                                                                                                 tiles, use_closure);
+        cl::k_step<<<(unsigned)(tiles * n_dom), cl::THREADS, cl::smem_fwd_bytes(), ctx->stream>>>(
+            theta, w2p, p, cur, alt, n, tiles, use_closure);
         std::swap(cur, alt);
     }
     SW_CUDA(ctx, cudaGetLastError());

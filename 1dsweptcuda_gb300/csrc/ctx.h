@@ -103,6 +103,7 @@ struct sw_ctx {
     unsigned *d_flags = nullptr;
     size_t n_flags = 0;
     int *d_status = nullptr;
+    void *d_w2p = nullptr;  // closure layer-2 weights, BF16, in the kernels' shared-memory layout
     void *h_pin = nullptr;
     size_t n_pin = 0;
     sw::BatchTables batch;

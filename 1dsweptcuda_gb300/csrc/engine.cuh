@@ -326,58 +326,52 @@ __device__ __forceinline__ void euler_level(const Params<T> &p, T *rows, int L, 
     }
 }
 
+// Which cell mapping a kernel carries: PATH_ANY picks at run time (blockDim.x
+// * 4 == W: 4 cells per thread), PATH_CELL and PATH_SPAN4 hold only one, so a
+// kernel does not pay the registers of a path it never runs.  Euler always
+// runs euler_level.
+enum TilePath { PATH_ANY = 0, PATH_CELL = 1, PATH_SPAN4 = 2 };
+
+// One sub-step of parity `par` on tile cells [lo, hi).  The one-cell-per-thread
+// loop starts at lo, so the live cells of a level start at the lowest thread:
+// whole warps idle, not part-empty ones.
+template <int P, typename T, int PATH>
+__device__ __forceinline__ void tile_level(const Params<T> &p, T *rows, int L, int W, int par, int lo, int hi,
+                                           Ends e) {
+    if constexpr (P == SW_EULER) {
+        euler_level<T>(p, rows, L, W, par, lo, hi, e);
+    } else if constexpr (PATH == PATH_SPAN4) {
+        tile_span4<P, T>(p, rows, L, par, lo, hi, e);
+    } else if constexpr (PATH == PATH_CELL) {
+        for (int x = lo + (int)threadIdx.x; x < hi; x += blockDim.x) tile_point<P, T>(p, rows, L, par, x, e);
+    } else {
+        if ((int)blockDim.x * 4 == W) {
+            tile_span4<P, T>(p, rows, L, par, lo, hi, e);
+        } else {
+            for (int x = lo + (int)threadIdx.x; x < hi; x += blockDim.x) tile_point<P, T>(p, rows, L, par, x, e);
+        }
+    }
+}
+
 // Down part: sub-steps j = 1..H on the growing centre [W/2 - jR, W/2 + jR).
-template <int P, typename T>
+template <int P, typename T, int PATH = PATH_ANY>
 __device__ __forceinline__ void tile_down(const Params<T> &p, T *rows, int L, int W, int64_t base) {
     constexpr int R = Scheme<P, T>::R;
     const int h = W >> 1, H = W / (2 * R);
     const Ends e = tile_ends(base, p.nx, W, R);
-    if constexpr (P == SW_EULER) {
-        for (int j = 1; j <= H; ++j) {
-            euler_level<T>(p, rows, L, W, j & 1, h - j * R, h + j * R, e);
-            __syncthreads();
-        }
-        return;
-    } else {
-        if ((int)blockDim.x * 4 == W) {
-            for (int j = 1; j <= H; ++j) {
-                tile_span4<P, T>(p, rows, L, j & 1, h - j * R, h + j * R, e);
-                __syncthreads();
-            }
-            return;
-        }
-    }
-    // the live cells of each level start at the lowest thread: whole warps idle, not part-empty ones
     for (int j = 1; j <= H; ++j) {
-        for (int x = h - j * R + (int)threadIdx.x; x < h + j * R; x += blockDim.x)
-            tile_point<P, T>(p, rows, L, j & 1, x, e);
+        tile_level<P, T, PATH>(p, rows, L, W, j & 1, h - j * R, h + j * R, e);
         __syncthreads();
     }
 }
 // Up part: sub-steps u = 1..H-1 on the shrinking [uR, W - uR).
-template <int P, typename T>
+template <int P, typename T, int PATH = PATH_ANY>
 __device__ __forceinline__ void tile_up(const Params<T> &p, T *rows, int L, int W, int64_t base) {
     constexpr int R = Scheme<P, T>::R;
     const int H = W / (2 * R);
     const Ends e = tile_ends(base, p.nx, W, R);
-    if constexpr (P == SW_EULER) {
-        for (int u = 1; u < H; ++u) {
-            euler_level<T>(p, rows, L, W, u & 1, u * R, W - u * R, e);
-            __syncthreads();
-        }
-        return;
-    } else {
-        if ((int)blockDim.x * 4 == W) {
-            for (int u = 1; u < H; ++u) {
-                tile_span4<P, T>(p, rows, L, u & 1, u * R, W - u * R, e);
-                __syncthreads();
-            }
-            return;
-        }
-    }
     for (int u = 1; u < H; ++u) {
-        for (int x = u * R + (int)threadIdx.x; x < W - u * R; x += blockDim.x)
-            tile_point<P, T>(p, rows, L, u & 1, x, e);
+        tile_level<P, T, PATH>(p, rows, L, W, u & 1, u * R, W - u * R, e);
         __syncthreads();
     }
 }
@@ -404,11 +398,10 @@ inline int swept_threads_for(int W, int threads) {
 // state and slots start at `state` and `slots`.  MODE_UP: state ->
 // up-triangle -> slots (phase 0 only).  MODE_DIAMOND: slots -> down + up ->
 // slots.  MODE_DOWN: slots -> down-triangle -> state.
-template <int P, typename T, int MODE>
+template <int P, typename T, int MODE, int PATH = PATH_ANY>
 __device__ __forceinline__ void swept_tile(const Params<T> &p, typename Scheme<P, T>::G *__restrict__ state,
                                            typename Scheme<P, T>::G *__restrict__ slots, T *rows, const int W,
                                            const int phase, const int64_t t) {
-    constexpr int R = Scheme<P, T>::R;
     const int L = row_stride(W), h = W >> 1;
     const int64_t nx = p.nx, nhalf = nx / h;
     const int64_t base = t * W + (int64_t)phase * h;
@@ -425,22 +418,22 @@ __device__ __forceinline__ void swept_tile(const Params<T> &p, typename Scheme<P
         tile_fix_bc<P, T>(p, rows, L, base);
     }
     __syncthreads();
-    if constexpr (MODE != MODE_UP) tile_down<P, T>(p, rows, L, W, base);
+    if constexpr (MODE != MODE_UP) tile_down<P, T, PATH>(p, rows, L, W, base);
     if constexpr (MODE == MODE_DOWN) {
         for (int x = threadIdx.x; x < W; x += blockDim.x) state[wrap_pos(base + x, nx)] = tile_get<P, T>(rows, L, 0, x);
     } else {
-        tile_up<P, T>(p, rows, L, W, base);
+        tile_up<P, T, PATH>(p, rows, L, W, base);
         tile_export<P, T>(rows, L, W, slots + hl * W, slots + hr * W);
     }
 }
 
 // One swept pass over all tiles of one domain; block = one tile.
-template <int P, typename T, int MODE>
+template <int P, typename T, int MODE, int PATH>
 __global__ void __launch_bounds__(Scheme<P, T>::MAXT) k_swept(const Params<T> p, typename Scheme<P, T>::G *__restrict__ state,
                                                 typename Scheme<P, T>::G *__restrict__ slots, const int W,
                                                 const int phase) {
     extern __shared__ __align__(16) unsigned char sw_smem[];
-    swept_tile<P, T, MODE>(p, state, slots, reinterpret_cast<T *>(sw_smem), W, phase, (int64_t)blockIdx.x);
+    swept_tile<P, T, MODE, PATH>(p, state, slots, reinterpret_cast<T *>(sw_smem), W, phase, (int64_t)blockIdx.x);
 }
 
 // One classic sub-step at cell g of a domain of p.nx cells: classicHeat
@@ -586,28 +579,37 @@ cudaError_t launch_classic(const void *vp, const void *in, void *out, int sub, i
     return cudaGetLastError();
 }
 
+template <int P, typename T, int PATH>
+cudaError_t launch_swept_path(const Params<T> &p, int mode, int phase, typename Scheme<P, T>::G *st,
+                              typename Scheme<P, T>::G *sl, int64_t nx, int W, int threads, cudaStream_t s) {
+    static bool configured = false;
+    if (!configured) {
+        allow_big_smem(k_swept<P, T, MODE_UP, PATH>);
+        allow_big_smem(k_swept<P, T, MODE_DIAMOND, PATH>);
+        allow_big_smem(k_swept<P, T, MODE_DOWN, PATH>);
+        configured = true;
+    }
+    const size_t smem = swept_smem_bytes<P, T>(W);
+    const unsigned grid = (unsigned)(nx / W);
+    switch (mode) {
+    case MODE_UP: k_swept<P, T, MODE_UP, PATH><<<grid, threads, smem, s>>>(p, st, sl, W, phase); break;
+    case MODE_DIAMOND: k_swept<P, T, MODE_DIAMOND, PATH><<<grid, threads, smem, s>>>(p, st, sl, W, phase); break;
+    default: k_swept<P, T, MODE_DOWN, PATH><<<grid, threads, smem, s>>>(p, st, sl, W, phase); break;
+    }
+    return cudaGetLastError();
+}
+
 template <int P, typename T>
 cudaError_t launch_swept(const void *vp, int mode, int phase, void *state, void *slots, int64_t nx, int W,
                          int threads_req, cudaStream_t s) {
     using G = typename Scheme<P, T>::G;
-    static bool configured = false;
-    if (!configured) {
-        allow_big_smem(k_swept<P, T, MODE_UP>);
-        allow_big_smem(k_swept<P, T, MODE_DIAMOND>);
-        allow_big_smem(k_swept<P, T, MODE_DOWN>);
-        configured = true;
-    }
     const Params<T> &p = *static_cast<const Params<T> *>(vp);
-    const size_t smem = swept_smem_bytes<P, T>(W);
-    const unsigned grid = (unsigned)(nx / W);
     const int threads = swept_threads_for<P, T>(W, threads_req);
     G *st = static_cast<G *>(state), *sl = static_cast<G *>(slots);
-    switch (mode) {
-    case MODE_UP: k_swept<P, T, MODE_UP><<<grid, threads, smem, s>>>(p, st, sl, W, phase); break;
-    case MODE_DIAMOND: k_swept<P, T, MODE_DIAMOND><<<grid, threads, smem, s>>>(p, st, sl, W, phase); break;
-    default: k_swept<P, T, MODE_DOWN><<<grid, threads, smem, s>>>(p, st, sl, W, phase); break;
+    if constexpr (P != SW_EULER) {
+        if (threads * 4 == W) return launch_swept_path<P, T, PATH_SPAN4>(p, mode, phase, st, sl, nx, W, threads, s);
     }
-    return cudaGetLastError();
+    return launch_swept_path<P, T, PATH_CELL>(p, mode, phase, st, sl, nx, W, threads, s);
 }
 
 template <typename T>

@@ -96,7 +96,7 @@ __device__ __forceinline__ void tile_import_cg(T *rows, int L, int W, const type
 
 // Stage q of tile t of one domain (state / slots / flags at the domain's
 // base).  Returns false if a wait gave up.
-template <int P, typename T>
+template <int P, typename T, int PATH>
 __device__ __forceinline__ bool persistent_tile(const Params<T> &p, typename Scheme<P, T>::G *__restrict__ state,
                                                 typename Scheme<P, T>::G *__restrict__ slots, unsigned *flags,
                                                 int *status, T *rows, const int W, const int64_t q,
@@ -118,13 +118,13 @@ __device__ __forceinline__ bool persistent_tile(const Params<T> &p, typename Sch
         tile_fix_bc<P, T>(p, rows, L, base);
     }
     __syncthreads();
-    if (q > 0) tile_down<P, T>(p, rows, L, W, base);
+    if (q > 0) tile_down<P, T, PATH>(p, rows, L, W, base);
     if (q == last) {
         for (int x = threadIdx.x; x < W; x += blockDim.x)
             state[wrap_pos(base + x, nx)] = tile_get<P, T>(rows, L, 0, x);
         __syncthreads();
     } else {
-        tile_up<P, T>(p, rows, L, W, base);
+        tile_up<P, T, PATH>(p, rows, L, W, base);
         tile_export<P, T>(rows, L, W, slots + hl * W, slots + hr * W);
         __threadfence();
         __syncthreads();
@@ -136,7 +136,7 @@ __device__ __forceinline__ bool persistent_tile(const Params<T> &p, typename Sch
     return true;
 }
 
-template <int P, typename T>
+template <int P, typename T, int PATH>
 __global__ void __launch_bounds__(Scheme<P, T>::MAXT)
     k_persistent(const Params<T> p, typename Scheme<P, T>::G *__restrict__ state,
                  typename Scheme<P, T>::G *__restrict__ slots, unsigned *__restrict__ flags, int *status, const int W,
@@ -146,14 +146,14 @@ __global__ void __launch_bounds__(Scheme<P, T>::MAXT)
     const int64_t ntile = p.nx / W, last = n_diamonds + 1;
     for (int64_t q = 0; q <= last; ++q)
         for (int64_t t = blockIdx.x; t < ntile; t += gridDim.x)
-            if (!persistent_tile<P, T>(p, state, slots, flags, status, rows, W, q, last, t)) return;
+            if (!persistent_tile<P, T, PATH>(p, state, slots, flags, status, rows, W, q, last, t)) return;
 }
 
 // ------------------------------------------------------------ ensembles
 // Many independent domains of uneven length in one launch (BatchDev, in
 // sw_internal.h, maps a global tile to its domain).
 
-template <int P, typename T, int MODE>
+template <int P, typename T, int MODE, int PATH>
 __global__ void __launch_bounds__(Scheme<P, T>::MAXT)
     k_swept_batch(const Params<T> p, typename Scheme<P, T>::G *__restrict__ state,
                   typename Scheme<P, T>::G *__restrict__ slots, const BatchDev b, const int W, const int phase) {
@@ -163,28 +163,29 @@ __global__ void __launch_bounds__(Scheme<P, T>::MAXT)
     const int64_t off = b.off[d];
     Params<T> q = p;
     q.nx = b.off[d + 1] - off;
-    swept_tile<P, T, MODE>(q, state + off, slots + 2 * off, reinterpret_cast<T *>(sw_smem), W, phase,
+    swept_tile<P, T, MODE, PATH>(q, state + off, slots + 2 * off, reinterpret_cast<T *>(sw_smem), W, phase,
                            g - b.tile0[d]);
 }
 
+// Classic step of an ensemble, one cell per thread, kClassicBlock threads per
+// block.  The table gives the domain of the block's first cell; each thread
+// walks forward from it, which is one compare when domains are longer than a
+// block.
 template <int P, typename T>
-__global__ void __launch_bounds__(Scheme<P, T>::MAXT)
+__global__ void __launch_bounds__(kClassicBlock)
     k_classic_batch(const Params<T> p, const typename Scheme<P, T>::G *__restrict__ in,
                     typename Scheme<P, T>::G *__restrict__ out, const BatchDev b, const int sub) {
-    const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t g = (int64_t)blockIdx.x * kClassicBlock + threadIdx.x;
     if (g >= b.n_cells) return;
-    int lo = 0, hi = b.n_dom;  // largest d with off[d] <= g
-    while (hi - lo > 1) {
-        const int mid = (lo + hi) >> 1;
-        if (b.off[mid] <= g) lo = mid; else hi = mid;
-    }
-    const int64_t off = b.off[lo];
+    int d = b.blk_dom[blockIdx.x];
+    while (b.off[d + 1] <= g) ++d;
+    const int64_t off = b.off[d];
     Params<T> q = p;
-    q.nx = b.off[lo + 1] - off;
+    q.nx = b.off[d + 1] - off;
     classic_cell<P, T>(q, in + off, out + off, sub, g - off);
 }
 
-template <int P, typename T>
+template <int P, typename T, int PATH>
 __global__ void __launch_bounds__(Scheme<P, T>::MAXT)
     k_persistent_batch(const Params<T> p, typename Scheme<P, T>::G *__restrict__ state,
                        typename Scheme<P, T>::G *__restrict__ slots, const BatchDev b, unsigned *__restrict__ flags,
@@ -198,19 +199,25 @@ __global__ void __launch_bounds__(Scheme<P, T>::MAXT)
             const int64_t off = b.off[d];
             Params<T> pp = p;
             pp.nx = b.off[d + 1] - off;
-            if (!persistent_tile<P, T>(pp, state + off, slots + 2 * off, flags + 2 * b.tile0[d], status, rows, W, q,
+            if (!persistent_tile<P, T, PATH>(pp, state + off, slots + 2 * off, flags + 2 * b.tile0[d], status, rows, W, q,
                                        last, g - b.tile0[d]))
                 return;
         }
     }
 }
 
+// The cell path a launch runs: 4 cells per thread when threads * 4 == W (not Euler).
 template <int P, typename T>
-cudaError_t launch_persistent(const void *vp, void *state, void *slots, unsigned *flags, int *status, int64_t nx,
-                              int W, int threads_req, int64_t n_diamonds, cudaStream_t s) {
-    using G = typename Scheme<P, T>::G;
+inline bool span4_launch(int W, int threads) {
+    return P != SW_EULER && threads * 4 == W;
+}
+
+template <int P, typename T, int PATH>
+cudaError_t launch_persistent_path(const Params<T> &p, typename Scheme<P, T>::G *st, typename Scheme<P, T>::G *sl,
+                                   unsigned *flags, int *status, int64_t nx, int W, int threads, int64_t n_diamonds,
+                                   cudaStream_t s) {
     static bool configured = false;
-    auto kern = k_persistent<P, T>;
+    auto kern = k_persistent<P, T, PATH>;
     const size_t smem = swept_smem_bytes<P, T>(W);
     if (!configured) {
         allow_big_smem(kern);
@@ -219,7 +226,6 @@ cudaError_t launch_persistent(const void *vp, void *state, void *slots, unsigned
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int threads = swept_threads_for<P, T>(W, threads_req);
     cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) return cudaErrorInvalidConfiguration;
@@ -229,37 +235,59 @@ cudaError_t launch_persistent(const void *vp, void *state, void *slots, unsigned
     const int64_t nhalf = nx / (W >> 1);
     e = cudaMemsetAsync(flags, 0, sizeof(unsigned) * nhalf, s);
     if (e != cudaSuccess) return e;
-    Params<T> p = *static_cast<const Params<T> *>(vp);
-    G *st = static_cast<G *>(state), *sl = static_cast<G *>(slots);
+    Params<T> pv = p;
     int Wv = W;
     int64_t nd = n_diamonds;
-    void *args[] = {&p, &st, &sl, &flags, &status, &Wv, &nd};
+    void *args[] = {&pv, &st, &sl, &flags, &status, &Wv, &nd};
     return cudaLaunchCooperativeKernel((const void *)kern, dim3((unsigned)grid), dim3(threads), args, smem, s);
+}
+
+template <int P, typename T>
+cudaError_t launch_persistent(const void *vp, void *state, void *slots, unsigned *flags, int *status, int64_t nx,
+                              int W, int threads_req, int64_t n_diamonds, cudaStream_t s) {
+    using G = typename Scheme<P, T>::G;
+    const Params<T> &p = *static_cast<const Params<T> *>(vp);
+    const int threads = swept_threads_for<P, T>(W, threads_req);
+    G *st = static_cast<G *>(state), *sl = static_cast<G *>(slots);
+    if (span4_launch<P, T>(W, threads))
+        return launch_persistent_path<P, T, PATH_SPAN4>(p, st, sl, flags, status, nx, W, threads, n_diamonds, s);
+    return launch_persistent_path<P, T, PATH_CELL>(p, st, sl, flags, status, nx, W, threads, n_diamonds, s);
+}
+
+template <int P, typename T, int PATH>
+cudaError_t launch_swept_batch_path(const Params<T> &p, int mode, int phase, typename Scheme<P, T>::G *st,
+                                    typename Scheme<P, T>::G *sl, const BatchDev &b, int W, int threads,
+                                    cudaStream_t s) {
+    static bool configured = false;
+    if (!configured) {
+        allow_big_smem(k_swept_batch<P, T, MODE_UP, PATH>);
+        allow_big_smem(k_swept_batch<P, T, MODE_DIAMOND, PATH>);
+        allow_big_smem(k_swept_batch<P, T, MODE_DOWN, PATH>);
+        configured = true;
+    }
+    const size_t smem = swept_smem_bytes<P, T>(W);
+    const unsigned grid = (unsigned)b.n_tiles;
+    switch (mode) {
+    case MODE_UP: k_swept_batch<P, T, MODE_UP, PATH><<<grid, threads, smem, s>>>(p, st, sl, b, W, phase); break;
+    case MODE_DIAMOND:
+        k_swept_batch<P, T, MODE_DIAMOND, PATH><<<grid, threads, smem, s>>>(p, st, sl, b, W, phase);
+        break;
+    default: k_swept_batch<P, T, MODE_DOWN, PATH><<<grid, threads, smem, s>>>(p, st, sl, b, W, phase); break;
+    }
+    return cudaGetLastError();
 }
 
 template <int P, typename T>
 cudaError_t launch_swept_batch(const void *vp, int mode, int phase, void *state, void *slots, const void *bt, int W,
                                int threads, cudaStream_t s) {
     using G = typename Scheme<P, T>::G;
-    static bool configured = false;
-    if (!configured) {
-        allow_big_smem(k_swept_batch<P, T, MODE_UP>);
-        allow_big_smem(k_swept_batch<P, T, MODE_DIAMOND>);
-        allow_big_smem(k_swept_batch<P, T, MODE_DOWN>);
-        configured = true;
-    }
     const Params<T> &p = *static_cast<const Params<T> *>(vp);
     const BatchDev &b = *static_cast<const BatchDev *>(bt);
     threads = swept_threads_for<P, T>(W, threads);
-    const size_t smem = swept_smem_bytes<P, T>(W);
     G *st = static_cast<G *>(state), *sl = static_cast<G *>(slots);
-    const unsigned grid = (unsigned)b.n_tiles;
-    switch (mode) {
-    case MODE_UP: k_swept_batch<P, T, MODE_UP><<<grid, threads, smem, s>>>(p, st, sl, b, W, phase); break;
-    case MODE_DIAMOND: k_swept_batch<P, T, MODE_DIAMOND><<<grid, threads, smem, s>>>(p, st, sl, b, W, phase); break;
-    default: k_swept_batch<P, T, MODE_DOWN><<<grid, threads, smem, s>>>(p, st, sl, b, W, phase); break;
-    }
-    return cudaGetLastError();
+    if (span4_launch<P, T>(W, threads))
+        return launch_swept_batch_path<P, T, PATH_SPAN4>(p, mode, phase, st, sl, b, W, threads, s);
+    return launch_swept_batch_path<P, T, PATH_CELL>(p, mode, phase, st, sl, b, W, threads, s);
 }
 
 template <int P, typename T>
@@ -268,28 +296,26 @@ cudaError_t launch_classic_batch(const void *vp, const void *in, void *out, int 
     using G = typename Scheme<P, T>::G;
     const Params<T> &p = *static_cast<const Params<T> *>(vp);
     const BatchDev &b = *static_cast<const BatchDev *>(bt);
-    if (block <= 0 || block > Scheme<P, T>::CMAXT) block = 256;
-    const int64_t grid = (b.n_cells + block - 1) / block;
-    k_classic_batch<P, T><<<(unsigned)grid, block, 0, s>>>(p, static_cast<const G *>(in), static_cast<G *>(out), b,
-                                                            sub);
+    (void)block;  // the block is fixed by the domain table's granularity
+    const int64_t grid = (b.n_cells + kClassicBlock - 1) / kClassicBlock;
+    k_classic_batch<P, T><<<(unsigned)grid, kClassicBlock, 0, s>>>(p, static_cast<const G *>(in), static_cast<G *>(out),
+                                                                    b, sub);
     return cudaGetLastError();
 }
 
 // Cooperative launch through cudaLaunchKernelEx so that it can be captured
 // into a CUDA graph.
-template <int P, typename T>
-cudaError_t launch_persistent_batch(const void *vp, void *state, void *slots, const void *bt, unsigned *flags,
-                                    int *status, int W, int threads, int64_t n_diamonds, cudaStream_t s) {
-    using G = typename Scheme<P, T>::G;
+template <int P, typename T, int PATH>
+cudaError_t launch_persistent_batch_path(const Params<T> &p, typename Scheme<P, T>::G *st,
+                                         typename Scheme<P, T>::G *sl, const BatchDev &b, unsigned *flags,
+                                         int *status, int W, int threads, int64_t n_diamonds, cudaStream_t s) {
     static bool configured = false;
-    auto kern = k_persistent_batch<P, T>;
+    auto kern = k_persistent_batch<P, T, PATH>;
     const size_t smem = swept_smem_bytes<P, T>(W);
     if (!configured) {
         allow_big_smem(kern);
         configured = true;
     }
-    threads = swept_threads_for<P, T>(W, threads);
-    const BatchDev &b = *static_cast<const BatchDev *>(bt);
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -310,8 +336,20 @@ cudaError_t launch_persistent_batch(const void *vp, void *state, void *slots, co
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, kern, *static_cast<const Params<T> *>(vp), static_cast<G *>(state),
-                              static_cast<G *>(slots), b, flags, status, W, n_diamonds);
+    return cudaLaunchKernelEx(&cfg, kern, p, st, sl, b, flags, status, W, n_diamonds);
+}
+
+template <int P, typename T>
+cudaError_t launch_persistent_batch(const void *vp, void *state, void *slots, const void *bt, unsigned *flags,
+                                    int *status, int W, int threads, int64_t n_diamonds, cudaStream_t s) {
+    using G = typename Scheme<P, T>::G;
+    const Params<T> &p = *static_cast<const Params<T> *>(vp);
+    const BatchDev &b = *static_cast<const BatchDev *>(bt);
+    threads = swept_threads_for<P, T>(W, threads);
+    G *st = static_cast<G *>(state), *sl = static_cast<G *>(slots);
+    if (span4_launch<P, T>(W, threads))
+        return launch_persistent_batch_path<P, T, PATH_SPAN4>(p, st, sl, b, flags, status, W, threads, n_diamonds, s);
+    return launch_persistent_batch_path<P, T, PATH_CELL>(p, st, sl, b, flags, status, W, threads, n_diamonds, s);
 }
 
 }  // namespace sw

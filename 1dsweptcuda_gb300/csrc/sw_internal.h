@@ -28,12 +28,14 @@ struct Params {
 // [2*tile0[d], ...); tile_dom maps a global tile of width W to its domain.
 struct BatchDev {
     const int32_t *tile_dom;
-    const int64_t *off;    // n_dom + 1 cell offsets
-    const int64_t *tile0;  // first global tile of each domain
+    const int64_t *off;      // n_dom + 1 cell offsets
+    const int64_t *tile0;    // first global tile of each domain
+    const int32_t *blk_dom;  // domain of the first cell of each kClassicBlock-cell classic block
     int64_t n_tiles;
     int64_t n_cells;
     int32_t n_dom;
 };
+constexpr int kClassicBlock = 256;  // threads (= cells) per block of the ensemble classic kernel
 
 // Swept launch modes.
 enum SweptMode { MODE_UP = 0, MODE_DIAMOND = 1, MODE_DOWN = 2 };

@@ -226,7 +226,8 @@ int sw_query_tuning(sw_ctx *ctx, const sw_config *cfg, int32_t n_domains, const 
 /* delta = f(u) for n_dom domains. */
 int sw_closure_infer(sw_ctx *ctx, const float *theta, const float *u, float *delta, int32_t n_dom, int64_t n);
 /* n_steps coarse KS steps (coarse: problem SW_KS, precision 4, its dt and dx)
- * fused with the closure (use_closure = 0: the plain coarse step), in place. */
+ * fused with the closure (use_closure = 0: the plain coarse step, theta may
+ * then be NULL), in place. */
 int sw_closure_step(sw_ctx *ctx, const sw_config *coarse, const float *theta, float *u, int32_t n_dom, int64_t n,
                     int64_t n_steps, int32_t use_closure, sw_result *out);
 /* Loss L = mean over points of (net(u) - target / s)^2 over the n_dom domains

@@ -159,3 +159,20 @@ def test_adaptive_estimate_tracks_error(sw, solver, cl):
     assert float(err.max()) < 1e-3, err
     assert float(est.max()) < 1e-3, est
     assert bool((err < 4 * est + 1e-6).all()), (err, est)
+
+
+def test_step_without_closure_needs_no_parameters(sw, solver, cl):
+    """sw_closure_step with the closure off takes a null theta (nothing reads it)."""
+    import ctypes as C
+    rng = np.random.default_rng(12)
+    u = (rng.standard_normal((2, 1024))).astype(np.float32)
+    t = torch.from_numpy(u.copy()).cuda()
+    c = cl.Closure(solver)
+    cfg = c.coarse_config()
+    res = sw.Result()
+    rc = sw.library().sw_closure_step(solver._ctx, C.byref(cfg), None, C.c_void_p(t.data_ptr()), 2, 1024, 3, 0,
+                                      C.byref(res))
+    assert rc == 0
+    want = torch.from_numpy(u.copy()).cuda()
+    c.step(want, 3, use_closure=False)
+    assert torch.equal(t, want)
