@@ -58,8 +58,12 @@ struct Scheme {
 
 // ---- shared-memory tile access: layout [row][component][L], cell x of a row at
 // index R + x.  L = W + 8 (>= W + 2R): every row starts 16-byte aligned and the
-// 8-value windows of the 4-cells-per-thread path never leave their row.
+// 8-value windows of the 4-cells-per-thread path never leave their row.  KS
+// also keeps rows 2 and 3, the squares of rows 0 and 1, for the
+// one-cell-per-thread path: every write of a value there writes its square.
 __host__ __device__ constexpr int row_stride(int W) { return W + 8; }
+template <int P>
+__host__ __device__ constexpr int tile_rows() { return P == SW_KS ? 4 : 2; }
 template <int P, typename T>
 __device__ __forceinline__ void tile_put(T *rows, int L, int row, int x, const typename Scheme<P, T>::G &v) {
     constexpr int R = Scheme<P, T>::R;
@@ -70,6 +74,7 @@ __device__ __forceinline__ void tile_put(T *rows, int L, int row, int x, const t
         b[2 * L] = v.z;
     } else {
         rows[row * L + R + x] = v;
+        if constexpr (P == SW_KS) rows[(2 + row) * L + R + x] = ml(v, v);
     }
 }
 template <int P, typename T>
@@ -117,10 +122,14 @@ __device__ __forceinline__ void tile_point(const Params<T> &p, T *rows, int L, i
         }
         dst[x] = heat_step(p, src[l], src[x], src[r]);
     } else if constexpr (P == SW_KS) {
+        const T *sq = rows + (2 + (par ^ 1)) * L + R;  // squares of the source row
+        T v;
         if (par)
-            dst[x] = ks_predict(p, src[x - 2], src[x - 1], src[x], src[x + 1], src[x + 2]);
+            v = ks_predict_sq(p, src[x - 2], src[x - 1], src[x], src[x + 1], src[x + 2], sq[x - 1], sq[x + 1]);
         else
-            dst[x] = ks_correct(p, dst[x], src[x - 2], src[x - 1], src[x], src[x + 1], src[x + 2]);
+            v = ks_correct_sq(p, dst[x], src[x - 2], src[x - 1], src[x], src[x + 1], src[x + 2], sq[x - 1], sq[x + 1]);
+        dst[x] = v;
+        rows[(2 + par) * L + R + x] = ml(v, v);
     } else {
         if (x == e.first || x == e.last) return;  // Dirichlet cells, Euler1D_SweptShared.cu:405-416
         const bool fl = (x == e.first + 1), fr = (x == e.last - 1);
@@ -141,7 +150,7 @@ __device__ __forceinline__ void tile_point(const Params<T> &p, T *rows, int L, i
 
 template <int P, typename T>
 __host__ __device__ constexpr size_t swept_smem_bytes(int W) {
-    return sizeof(T) * 2 * Scheme<P, T>::C * (size_t)row_stride(W);
+    return sizeof(T) * tile_rows<P>() * Scheme<P, T>::C * (size_t)row_stride(W);
 }
 
 __device__ __forceinline__ int64_t wrap_pos(int64_t q, int64_t nx) {

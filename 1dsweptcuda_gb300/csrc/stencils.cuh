@@ -50,12 +50,16 @@ __device__ __forceinline__ T heat_step(const Params<T> &p, T l, T c, T r) {
 // reference's expression while the FP64 pipe does 15 operations instead of 20
 // (barring overflow or underflow of the scaled terms, ~1e+-300).
 template <typename T>
-__device__ __forceinline__ T ks_rhs(const Params<T> &p, T ll, T l, T c, T r, T rr) {
-    const T conv = sb(ml(r, r), ml(l, l));
+__device__ __forceinline__ T ks_rhs_sq(const Params<T> &p, T ll, T l, T c, T r, T rr, T l2, T r2) {
+    const T conv = sb(r2, l2);  // l2 = l*l, r2 = r*r
     const T sec = fm(T(-2), c, ad(l, r));                        // (l + r) - 2c
     const T fourth = ad(fm(T(-4), r, ad(fm(T(-4), l, ll), ml(T(6), c))), rr);  // ((ll - 4l) + 6c) - 4r + rr
     if (p.pow2) return fm(fourth, p.d4, fm(conv, p.c4, ml(sec, p.d2)));
     return ad(ad(ml(conv, p.c4), ml(sec, p.d2)), ml(fourth, p.d4));
+}
+template <typename T>
+__device__ __forceinline__ T ks_rhs(const Params<T> &p, T ll, T l, T c, T r, T rr) {
+    return ks_rhs_sq(p, ll, l, c, r, rr, ml(l, l), ml(r, r));
 }
 // stutterStep, KS1D_SweptShared.cu:159-164: u - dt/2 * rhs
 template <typename T>
@@ -66,6 +70,17 @@ __device__ __forceinline__ T ks_predict(const Params<T> &p, T ll, T l, T c, T r,
 template <typename T>
 __device__ __forceinline__ T ks_correct(const Params<T> &p, T u, T ll, T l, T c, T r, T rr) {
     return ad(u, ml(-p.dt, ks_rhs(p, ll, l, c, r, rr)));
+}
+// The same with the squares l*l and r*r of the neighbours supplied (each cell's
+// square is then formed once, by the thread that produced the value, instead
+// of by both of its neighbours; the product is the same __dmul_rn either way).
+template <typename T>
+__device__ __forceinline__ T ks_predict_sq(const Params<T> &p, T ll, T l, T c, T r, T rr, T l2, T r2) {
+    return sb(c, ml(p.dth, ks_rhs_sq(p, ll, l, c, r, rr, l2, r2)));
+}
+template <typename T>
+__device__ __forceinline__ T ks_correct_sq(const Params<T> &p, T u, T ll, T l, T c, T r, T rr, T l2, T r2) {
+    return ad(u, ml(-p.dt, ks_rhs_sq(p, ll, l, c, r, rr, l2, r2)));
 }
 
 // --------------------------------------------------------------- Euler

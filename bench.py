@@ -40,13 +40,18 @@ DT = 0.005
 TF = 200.0
 NSTEPS = 40000            # tf / dt
 B_CLASSIC_KS_F64 = 40     # algorithmic bytes per cell-update of the classic KS FP64 scheme
-DP_OPS_PER_UPDATE = 30    # FP64 instructions per cell-update: 2 sub-steps x 15 (exact power-of-two folds)
+# FP64 operations per cell-update of the swept cell path: 2 sub-steps x 14 (exact power-of-two
+# folds; each cell's square formed once and shared with both neighbours): 5 FMA, 4 MUL, 5 ADD.
+DP_OPS_PER_UPDATE = 28
 # FP64 pipe issue rates of this GB300 pool, measured with a throughput probe
 # (152 SMs at 2.07 GHz): DFMA 0.627e12/s (1.99 per clock per SM, 1.25 TFLOP/s),
-# DADD and DMUL 0.528e12/s.  A KS sub-step is 5 FMA + 5 MUL + 5 ADD, so its
-# mix issues at 15 / (5 / 0.627 + 10 / 0.528) = 0.557e12 operations/s.
+# DADD and DMUL 0.528e12/s.  The swept KS sub-step's mix (5 FMA, 9 MUL/ADD)
+# issues at 14 / (5 / 0.627 + 9 / 0.528) = 0.560e12 operations/s.
 FP64_OPS_PEAK = 0.627e12
-FP64_KS_MIX_PEAK = 15.0 / (5.0 / 0.627e12 + 10.0 / 0.528e12)
+FP64_KS_MIX_PEAK = 14.0 / (5.0 / 0.627e12 + 9.0 / 0.528e12)
+METRIC = "cell-updates/s (KS1D FP64 swept, nx=2^20, tpb=256, dt=0.005, tf=200)"
+WORKLOAD = ("KS1D FP64 swept (alg 1), periodic, nx=2^20, tpb=256, dx=0.5, dt=0.005, tf=200 "
+            "(40000 time steps per step)")
 K40_KS_F64_SWEPT_PUBLISHED = 1.07e10  # the reference's published KS FP64 swept figure, nx=2^20, on a K40c
 # DRAM bytes (read + write) of one diamond launch of this workload from one ncu
 # capture of this launch (cold-cache replay).
@@ -173,12 +178,14 @@ def run_reference(args) -> None:
     wall = time.perf_counter() - t_all
     v = statistics.median([x["value"] for x in vals])
     line = {
-        "impl": "reference", "metric": "cell-updates/s (KS1D FP64, nx=2^20, tpb=256, dt=0.005, tf=200)",
+        "impl": "reference", "metric": METRIC,
         "value": v, "unit": "cell-updates/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": wall * 1e3 / max(1, args.steps), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic: reference KS IC 2cos(19 pi x/128)",
-        "config": {"workload": "KS1D FP64 classic (reference scheme on host cores), nx=2^20, dt=0.005",
-                   "note": "the reference's programs need a GPU; this arm is the C/OpenMP port of its classic scheme"},
+        "config": {"workload": WORKLOAD, "nx": NX, "tpb": TPB, "time_steps_per_step": NSTEPS,
+                   "note": "the reference's programs need a GPU; this arm times the C/OpenMP port of its classic "
+                           "scheme (the same cell-updates, bit for bit) on the host cores, on a bounded sample "
+                           "of the time steps"},
         "cpu_baseline": {"value": v, "unit": "cell-updates/s", "cores": vals[0]["cores"], "kind": "port",
                          "sample": vals[0]["sample"]},
         "e2e": {"value": v, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -292,13 +299,12 @@ def run_ours(args) -> None:
 
     base = cpu_baseline(seconds=10.0) if world == 1 else None
     line = {
-        "metric": "cell-updates/s (KS1D FP64 swept, nx=2^20, tpb=256, dt=0.005, tf=200)",
+        "metric": METRIC,
         "value": value, "unit": "cell-updates/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": value / K40_KS_F64_SWEPT_PUBLISHED, "dtype": "f64",
         "data": "synthetic: the reference KS IC u(x,0) = 2cos(19 pi x/128)",
-        "config": {"workload": "KS1D FP64 swept (alg 1), periodic, nx=2^20, tpb=256, dx=0.5, dt=0.005, tf=200 "
-                               "(40000 time steps per step), state resident in HBM",
+        "config": {"workload": WORKLOAD + ", state resident in HBM",
                    "nx": NX, "tpb": TPB, "time_steps_per_step": NSTEPS, "alg": "swept",
                    "l2": "flushed between steps (256 MiB write), outside the step timing",
                    "vs_baseline_source": "the reference's published KS FP64 swept figure, nx=2^20, K40c: 1.07e10 cell-updates/s"},
