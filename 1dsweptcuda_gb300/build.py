@@ -29,7 +29,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # operation with a round-to-nearest intrinsic, so they never depend on it.
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC",
                      "-Xptxas", "-warn-spills", "-I", str(INCLUDE)]
-CU_SOURCES = ["k_heat.cu", "k_ks.cu", "k_euler.cu", "api.cu", "batch.cu", "noalloc.cu", "closure.cu"]
+CU_SOURCES = ["k_heat.cu", "k_ks.cu", "k_euler.cu", "api.cu", "batch.cu", "noalloc.cu", "closure.cu", "diag.cu"]
 CPP_SOURCES = ["cli.cpp"]
 HEADERS = ["engine.cuh", "stencils.cuh", "persistent.cuh", "sw_internal.h", "ctx.h"]
 PROGRAMS = [(p, pi, q, qi) for pi, p in enumerate(("Heat", "KS", "Euler")) for q, qi in (("Single", 4), ("Double", 8))]

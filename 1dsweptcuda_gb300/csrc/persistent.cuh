@@ -41,16 +41,19 @@ __device__ __forceinline__ uint64_t global_ns() {
 }
 
 // Thread 0 waits for both slot flags to reach `need`; returns false (and sets
-// *status) if the wait runs out or another block already failed.
+// *status) if the wait runs out or another block already failed.  The wait
+// ends after limit_ns of %globaltimer, or after limit_ns / 16 polls (each
+// sleeps >= 64 ns, so >= 4 x limit_ns) should the timer ever stand still.
 __device__ __forceinline__ bool wait_slots(const unsigned *flags, int64_t hl, int64_t hr, unsigned need,
-                                           volatile int *status) {
+                                           volatile int *status, uint64_t limit_ns = SW_WAIT_NS) {
     __shared__ int ok;
     if (threadIdx.x == 0) {
         int good = 1;
-        const uint64_t t0 = global_ns();
+        const uint64_t t0 = global_ns(), max_polls = limit_ns / 16;
+        uint64_t polls = 0;
         while (ld_acquire_u32(flags + hl) < need || ld_acquire_u32(flags + hr) < need) {
             if (*status != 0) { good = 0; break; }
-            if (global_ns() - t0 > SW_WAIT_NS) {
+            if (global_ns() - t0 > limit_ns || ++polls > max_polls) {
                 atomicCAS((int *)status, 0, 1);
                 good = 0;
                 break;

@@ -29,7 +29,7 @@ EXPORTED = ["sw_abi_version", "sw_strerror", "sw_ctx_create", "sw_ctx_destroy", 
             "sw_config_init", "sw_validate", "sw_constants_of", "sw_initial_condition", "sw_run",
             "sw_run_device", "sw_plan", "sw_cli_main", "sw_run_batch", "sw_run_batch_device",
             "sw_query_tuning", "sw_run_device_noalloc", "sw_closure_infer", "sw_closure_step",
-            "sw_closure_grad", "sw_closure_adam", "sw_closure_train", "sw_coarse_grain"]
+            "sw_closure_grad", "sw_closure_adam", "sw_closure_train", "sw_coarse_grain", "sw_wait_probe"]
 CLOSURE_PARAMS = 5506
 NOALLOC_SCRATCH_BYTES = 24 * 1024 * 1024
 
@@ -133,6 +133,7 @@ def library():
     L.sw_closure_train.argtypes = [vp, vp, vp, vp, C.c_int64, C.c_int64, C.c_int32, C.c_int32, C.c_float,
                                    C.c_uint64, C.POINTER(C.c_float)]
     L.sw_coarse_grain.argtypes = [vp, vp, vp, C.c_int64, C.c_int32]
+    L.sw_wait_probe.argtypes = [vp, C.c_int64, C.POINTER(C.c_double)]
     for name in ("sw_ctx_create", "sw_ctx_destroy", "sw_config_init", "sw_validate", "sw_constants_of",
                  "sw_initial_condition", "sw_run", "sw_run_device", "sw_cli_main", "sw_plan", "sw_run_batch",
                  "sw_run_batch_device", "sw_query_tuning", "sw_run_device_noalloc", "sw_closure_infer",
@@ -292,8 +293,15 @@ class _BatchMixin:
             raise self._err(rc, "sw_query_tuning")
         return t
 
+    def wait_probe(self, limit_ns: int) -> tuple[int, float]:
+        """sw_wait_probe: run the bounded wait on a flag nothing sets; returns
+        (status code, milliseconds waited).  SW_ERR_TIMEOUT (-7) is the expected code."""
+        ms = C.c_double(0.0)
+        rc = self._lib.sw_wait_probe(self._ctx, int(limit_ns), C.byref(ms))
+        return rc, ms.value
 
-for _name in ("run_batch", "run_batch_device", "tune"):
+
+for _name in ("run_batch", "run_batch_device", "tune", "wait_probe"):
     setattr(Solver, _name, getattr(_BatchMixin, _name))
 
 

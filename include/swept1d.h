@@ -274,6 +274,12 @@ int sw_coarse_grain(sw_ctx *ctx, const double *fine, float *coarse, int64_t n_co
 #define SW_NOALLOC_SCRATCH_BYTES (24u * 1024u * 1024u)
 int sw_run_device_noalloc(const sw_config *cfg, void *state_dev, void *stream);
 
+/* Failure-path check (no reference counterpart): runs the persistent kernels'
+ * bounded wait on a flag that nothing sets, with a limit of limit_ns
+ * (1e6..1e10 ns).  Returns SW_ERR_TIMEOUT once the wait has run out, with the
+ * wait's duration in *waited_ms (may be NULL); the context stays usable. */
+int sw_wait_probe(sw_ctx *ctx, int64_t limit_ns, double *waited_ms);
+
 /* The whole program: argv exactly as bin/<Problem><Precision>Out takes it
  * (replaces main(), Heat1D_SweptShared.cu:697-836, KS1D_SweptShared.cu:866-1029,
  * Euler1D_SweptShared.cu:1112-1287).  Writes solution.dat and appends the

@@ -207,3 +207,18 @@ def test_euler_device_layout(sw, solver, oracle):
     out = t.cpu().numpy()
     _assert_identical(np.ascontiguousarray(out[:, :3]).ravel(), oracle.classic(c, ic, 96), "euler device")
     assert (out[:, 3] == 0).all()
+
+
+def test_bounded_wait_reports_timeout(sw, solver, oracle):
+    """The persistent kernels' wait, on a flag nothing sets, gives up after its
+    limit and reports SW_ERR_TIMEOUT through the status word; the context then
+    runs a solve normally."""
+    rc, ms = solver.wait_probe(50_000_000)  # 50 ms
+    assert rc == -7, rc
+    assert 40.0 < ms < 2000.0, ms
+    nx, dt = 256, 0.005
+    c = _case(oracle, KS, 8, nx, dt)
+    ic = _ic(oracle, KS, 8, nx)
+    got, _ = _gpu(sw, solver, KS, 8, VARIANT, nx, 64, dt, 40, ic)
+    _assert_identical(got, oracle.classic(c, ic, 40), "after the timeout")
+    assert solver.wait_probe(10)[0] == -1  # limit out of range: SW_ERR_ARG, nothing launched
