@@ -18,6 +18,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstddef>
 #include <cstdint>
@@ -444,16 +445,21 @@ int closure_check(sw_ctx *ctx, int32_t n_dom, int64_t n) {
     return SW_OK;
 }
 
+// The kernels' shared-memory limits, once per device (the attribute belongs to
+// the current device): a bit per device 0..63, set again on every call above.
 cudaError_t allow_smem() {
-    static bool done = false;
-    if (done) return cudaSuccess;
-    cudaError_t e =
-        cudaFuncSetAttribute(cl::k_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cl::smem_fwd_bytes());
+    static std::atomic<uint64_t> done{0};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    const uint64_t bit = (dev >= 0 && dev < 64) ? (uint64_t(1) << dev) : 0;
+    if (bit && (done.load(std::memory_order_acquire) & bit)) return cudaSuccess;
+    e = cudaFuncSetAttribute(cl::k_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cl::smem_fwd_bytes());
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(cl::k_step, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cl::smem_fwd_bytes());
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(cl::k_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cl::smem_bytes());
-    done = (e == cudaSuccess);
+    if (e == cudaSuccess) done.fetch_or(bit, std::memory_order_release);
     return e;
 }
 

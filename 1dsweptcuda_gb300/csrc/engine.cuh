@@ -28,6 +28,7 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <climits>
 #include <cstdint>
 #include <type_traits>
@@ -566,10 +567,27 @@ __global__ void k_unpack3(const V4<T> *__restrict__ in4, T *__restrict__ out3, i
 }
 
 // ------------------------------------------------------------- launchers
-template <typename K>
-inline void allow_big_smem(K kernel) {
-    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-}
+// The dynamic shared-memory limit above the 48 KB default, set once per
+// (launcher, device): the attribute belongs to the device that is current when
+// it is set, so the record is a bit per device (devices 0..63; a higher index
+// sets it on every call).  Setting it twice is harmless, so threads may race.
+struct SmemOnce {
+    std::atomic<uint64_t> done{0};
+    template <typename... K>
+    cudaError_t ensure(K... kernels) {
+        int dev = 0;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (e != cudaSuccess) return e;
+        const uint64_t bit = (dev >= 0 && dev < 64) ? (uint64_t(1) << dev) : 0;
+        if (bit && (done.load(std::memory_order_acquire) & bit)) return cudaSuccess;
+        for (auto k : {(const void *)kernels...}) {
+            e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+            if (e != cudaSuccess) return e;
+        }
+        done.fetch_or(bit, std::memory_order_release);
+        return cudaSuccess;
+    }
+};
 
 template <int P, typename T>
 cudaError_t launch_classic(const void *vp, const void *in, void *out, int sub, int64_t nx, int block,
@@ -591,13 +609,10 @@ cudaError_t launch_classic(const void *vp, const void *in, void *out, int sub, i
 template <int P, typename T, int PATH>
 cudaError_t launch_swept_path(const Params<T> &p, int mode, int phase, typename Scheme<P, T>::G *st,
                               typename Scheme<P, T>::G *sl, int64_t nx, int W, int threads, cudaStream_t s) {
-    static bool configured = false;
-    if (!configured) {
-        allow_big_smem(k_swept<P, T, MODE_UP, PATH>);
-        allow_big_smem(k_swept<P, T, MODE_DIAMOND, PATH>);
-        allow_big_smem(k_swept<P, T, MODE_DOWN, PATH>);
-        configured = true;
-    }
+    static SmemOnce once;
+    cudaError_t e = once.ensure(k_swept<P, T, MODE_UP, PATH>, k_swept<P, T, MODE_DIAMOND, PATH>,
+                                k_swept<P, T, MODE_DOWN, PATH>);
+    if (e != cudaSuccess) return e;
     const size_t smem = swept_smem_bytes<P, T>(W);
     const unsigned grid = (unsigned)(nx / W);
     switch (mode) {

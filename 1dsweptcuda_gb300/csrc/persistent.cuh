@@ -219,17 +219,15 @@ template <int P, typename T, int PATH>
 cudaError_t launch_persistent_path(const Params<T> &p, typename Scheme<P, T>::G *st, typename Scheme<P, T>::G *sl,
                                    unsigned *flags, int *status, int64_t nx, int W, int threads, int64_t n_diamonds,
                                    cudaStream_t s) {
-    static bool configured = false;
+    static SmemOnce once;
     auto kern = k_persistent<P, T, PATH>;
     const size_t smem = swept_smem_bytes<P, T>(W);
-    if (!configured) {
-        allow_big_smem(kern);
-        configured = true;
-    }
+    cudaError_t e = once.ensure(kern);
+    if (e != cudaSuccess) return e;
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) return cudaErrorInvalidConfiguration;
     const int64_t ntile = nx / W;
@@ -261,13 +259,10 @@ template <int P, typename T, int PATH>
 cudaError_t launch_swept_batch_path(const Params<T> &p, int mode, int phase, typename Scheme<P, T>::G *st,
                                     typename Scheme<P, T>::G *sl, const BatchDev &b, int W, int threads,
                                     cudaStream_t s) {
-    static bool configured = false;
-    if (!configured) {
-        allow_big_smem(k_swept_batch<P, T, MODE_UP, PATH>);
-        allow_big_smem(k_swept_batch<P, T, MODE_DIAMOND, PATH>);
-        allow_big_smem(k_swept_batch<P, T, MODE_DOWN, PATH>);
-        configured = true;
-    }
+    static SmemOnce once;
+    cudaError_t e = once.ensure(k_swept_batch<P, T, MODE_UP, PATH>, k_swept_batch<P, T, MODE_DIAMOND, PATH>,
+                                k_swept_batch<P, T, MODE_DOWN, PATH>);
+    if (e != cudaSuccess) return e;
     const size_t smem = swept_smem_bytes<P, T>(W);
     const unsigned grid = (unsigned)b.n_tiles;
     switch (mode) {
@@ -312,17 +307,15 @@ template <int P, typename T, int PATH>
 cudaError_t launch_persistent_batch_path(const Params<T> &p, typename Scheme<P, T>::G *st,
                                          typename Scheme<P, T>::G *sl, const BatchDev &b, unsigned *flags,
                                          int *status, int W, int threads, int64_t n_diamonds, cudaStream_t s) {
-    static bool configured = false;
+    static SmemOnce once;
     auto kern = k_persistent_batch<P, T, PATH>;
     const size_t smem = swept_smem_bytes<P, T>(W);
-    if (!configured) {
-        allow_big_smem(kern);
-        configured = true;
-    }
+    cudaError_t e = once.ensure(kern);
+    if (e != cudaSuccess) return e;
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) return cudaErrorInvalidConfiguration;
     int64_t grid = (int64_t)per_sm * sms;
