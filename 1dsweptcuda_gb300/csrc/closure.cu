@@ -33,6 +33,7 @@ namespace sw {
 namespace cl {
 
 constexpr int CH = 32, KW = 5;
+static_assert(CH == 32, "layer 1 maps one warp lane to each channel");
 constexpr int TOUT = 128;
 constexpr int NU = TOUT + 24;   // 152 input cells
 constexpr int NA1 = TOUT + 20;  // 148 a1 rows
@@ -130,13 +131,31 @@ __device__ void load_tile(Smem &s, const float *__restrict__ theta, const float 
 // TRAIN also the pre-activations z1 and z2.  Requires load_tile and a barrier first.
 template <bool TRAIN>
 __device__ void forward_12(Smem &s) {
-    for (int k = threadIdx.x; k < NA1 * CH; k += blockDim.x) {
-        const int r = k / CH, o = k % CH;
-        float z = s.b1[o];
+    {
+        // lane = output channel o; each warp a contiguous run of rows, with o's
+        // five weights and a sliding window of five inputs in registers (one
+        // shared load per row; the FMA chain is the same, tap 0 first)
+        const int o = threadIdx.x & 31, nw = blockDim.x >> 5;
+        const int per = (NA1 + nw - 1) / nw, r0 = (threadIdx.x >> 5) * per;
+        const int r1 = min(r0 + per, NA1);
+        float w[KW], u[KW];
 #pragma unroll
-        for (int t = 0; t < KW; ++t) z = fmaf(s.w1[o * KW + t], s.us[r + t], z);
-        if (TRAIN) s.z1[r * LDF + o] = z;
-        s.a1[r * LDB + o] = __float2bfloat16_rn(gelu(z));
+        for (int t = 0; t < KW; ++t) w[t] = s.w1[o * KW + t];
+        const float b = s.b1[o];
+        if (r0 < r1) {
+#pragma unroll
+            for (int t = 0; t < KW - 1; ++t) u[t + 1] = s.us[r0 + t];
+        }
+        for (int r = r0; r < r1; ++r) {
+#pragma unroll
+            for (int t = 0; t < KW - 1; ++t) u[t] = u[t + 1];
+            u[KW - 1] = s.us[r + KW - 1];
+            float z = b;
+#pragma unroll
+            for (int t = 0; t < KW; ++t) z = fmaf(w[t], u[t], z);
+            if (TRAIN) s.z1[r * LDF + o] = z;
+            s.a1[r * LDB + o] = __float2bfloat16_rn(gelu(z));
+        }
     }
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, q = lane & 3;
