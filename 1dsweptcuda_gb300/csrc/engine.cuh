@@ -107,14 +107,14 @@ __device__ __forceinline__ Ends tile_ends(int64_t base, int64_t nx, int W, int R
     return Ends{tile_coord_of(0, base, nx, -R, W + R), tile_coord_of(nx - 1, base, nx, -R, W + R)};
 }
 
-// One sub-step of parity `par` (1: predictor / odd Heat step; 0: corrector /
-// even Heat step) at tile cell x.
+// One Heat / KS sub-step of parity `par` (1: predictor / odd Heat step; 0:
+// corrector / even Heat step) at tile cell x.  (Euler levels run euler_level.)
 template <int P, typename T>
 __device__ __forceinline__ void tile_point(const Params<T> &p, T *rows, int L, int par, int x, Ends e) {
+    static_assert(P != SW_EULER, "Euler tile levels share interfaces across a warp (euler_level)");
     constexpr int R = Scheme<P, T>::R;
-    constexpr int C = Scheme<P, T>::C;
-    const T *src = rows + (par ^ 1) * C * L + R;
-    T *dst = rows + par * C * L + R;
+    const T *src = rows + (par ^ 1) * L + R;
+    T *dst = rows + par * L + R;
     if constexpr (P == SW_HEAT) {
         int l = x - 1, r = x + 1;
         if (p.bc != SW_BC_PERIODIC) {  // insulated ends, Heat1D_SweptShared.cu:140-142,352-353
@@ -131,21 +131,6 @@ __device__ __forceinline__ void tile_point(const Params<T> &p, T *rows, int L, i
             v = ks_correct_sq(p, dst[x], src[x - 2], src[x - 1], src[x], src[x + 1], src[x + 2], sq[x - 1], sq[x + 1]);
         dst[x] = v;
         rows[(2 + par) * L + R + x] = ml(v, v);
-    } else {
-        if (x == e.first || x == e.last) return;  // Dirichlet cells, Euler1D_SweptShared.cu:405-416
-        const bool fl = (x == e.first + 1), fr = (x == e.last - 1);
-        Q3<T> s[5];
-#pragma unroll
-        for (int k = 0; k < 5; ++k) s[k] = q3(src[x - 2 + k], src[L + x - 2 + k], src[2 * L + x - 2 + k]);
-        Q3<T> o;
-        if (par) {
-            o = eu_predict(p, s, fl, fr);
-        } else {
-            o = eu_correct(p, q3(dst[x], dst[L + x], dst[2 * L + x]), s, fl, fr);
-        }
-        dst[x] = o.x;
-        dst[L + x] = o.y;
-        dst[2 * L + x] = o.z;
     }
 }
 
