@@ -608,6 +608,121 @@ cudaError_t launch_swept_path(const Params<T> &p, int mode, int phase, typename 
     return cudaGetLastError();
 }
 
+// ------------------------------------------------ KS 128-cell tiles in one warp
+// FP32 KS swept with W = 128: one warp per tile, 8 tiles per block, the tile's
+// rows in registers -- lane l holds cells 4l .. 4l + 3 of row 0 (u) and row 1
+// (the predictor u*) and their squares, and row-1 cells -2, -1, 128, 129 (read
+// only by the last down level) sit in four more registers of every lane.  A
+// cell's neighbours are the lane's own registers or the next lane's, by
+// shuffles, so a level needs no barrier.  Slots, modes, level ranges and
+// arithmetic (ks_*_sq) are those of swept_tile with W = 128: the results are
+// the same bit for bit.
+constexpr int kKsWarpTile = 128;
+constexpr int kKsWarpTilesPerBlock = 8;
+
+// One sub-step of parity `par` on tile cells [lo, hi).
+template <typename T>
+__device__ __forceinline__ void ks_warp4_level(const Params<T> &p, int par, int lo, int hi, T (&u0)[4], T (&u1)[4],
+                                               T (&s0)[4], T (&s1)[4], const T (&m)[4], const T (&ms)[4]) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31, c0 = 4 * lane;
+    const T *src = par ? u0 : u1, *sq = par ? s0 : s1;
+    // the previous lane's cells 2, 3 and square 3; the next lane's cells 0, 1 and square 0
+    T pm2 = __shfl_up_sync(full, src[2], 1), pm1 = __shfl_up_sync(full, src[3], 1);
+    T pq1 = __shfl_up_sync(full, sq[3], 1);
+    T np0 = __shfl_down_sync(full, src[0], 1), np1 = __shfl_down_sync(full, src[1], 1);
+    T nq0 = __shfl_down_sync(full, sq[0], 1);
+    if (!par) {  // row-1 cells -2, -1 and 128, 129
+        if (lane == 0) { pm2 = m[0]; pm1 = m[1]; pq1 = ms[1]; }
+        if (lane == 31) { np0 = m[2]; np1 = m[3]; nq0 = ms[2]; }
+    }
+    const T w[8] = {pm2, pm1, src[0], src[1], src[2], src[3], np0, np1};  // cells c0 - 2 .. c0 + 5
+    const T q[6] = {pq1, sq[0], sq[1], sq[2], sq[3], nq0};                // squares of cells c0 - 1 .. c0 + 4
+    T v[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+        v[k] = par ? ks_predict_sq(p, w[k], w[k + 1], w[k + 2], w[k + 3], w[k + 4], q[k], q[k + 2])
+                   : ks_correct_sq(p, u0[k], w[k], w[k + 1], w[k + 2], w[k + 3], w[k + 4], q[k], q[k + 2]);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        if (c0 + k >= lo && c0 + k < hi) {
+            if (par) { u1[k] = v[k]; s1[k] = ml(v[k], v[k]); }
+            else { u0[k] = v[k]; s0[k] = ml(v[k], v[k]); }
+        }
+    }
+}
+
+template <typename T, int MODE>
+__global__ void __launch_bounds__(32 * kKsWarpTilesPerBlock)
+    k_swept_ks_warp(const Params<T> p, T *__restrict__ state, T *__restrict__ slots, const int phase) {
+    constexpr int W = kKsWarpTile, h = W / 2, R = 2, H = W / (2 * R);
+    const int lane = threadIdx.x & 31, c0 = 4 * lane;
+    const int64_t nx = p.nx, ntile = nx / W, nhalf = nx / h;
+    const int64_t t = (int64_t)blockIdx.x * kKsWarpTilesPerBlock + (threadIdx.x >> 5);
+    if (t >= ntile) return;  // whole warps: t is the same for the 32 lanes
+    const int64_t base = t * W + (int64_t)phase * h;
+    const int64_t hl = (2 * t + phase) % nhalf;
+    const int64_t hr = (hl + 1 == nhalf) ? 0 : hl + 1;
+    T *sl = slots + hl * W, *sr = slots + hr * W;
+    T u0[4], u1[4] = {T(0), T(0), T(0), T(0)}, m[4] = {T(0), T(0), T(0), T(0)};
+    if constexpr (MODE == MODE_UP) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) u0[k] = state[base + c0 + k];
+    } else {
+        // slot layout as tile_import: sl = [row 0, cells 0..63][row 1, cells -2..61],
+        // sr = [row 0, cells 64..127][row 1, cells 66..129]
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int c = c0 + k;
+            u0[k] = c < h ? sl[c] : sr[c - h];
+            if (c < h - R) u1[k] = sl[h + c + R];
+            else if (c >= h + R) u1[k] = sr[c - R];
+        }
+        m[0] = sl[h];
+        m[1] = sl[h + 1];
+        m[2] = sr[W - 2];
+        m[3] = sr[W - 1];
+    }
+    T s0[4], s1[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        s0[k] = ml(u0[k], u0[k]);
+        s1[k] = ml(u1[k], u1[k]);
+    }
+    const T ms[4] = {ml(m[0], m[0]), ml(m[1], m[1]), ml(m[2], m[2]), ml(m[3], m[3])};
+    if constexpr (MODE != MODE_UP) {
+        for (int j = 1; j <= H; ++j) ks_warp4_level(p, j & 1, h - j * R, h + j * R, u0, u1, s0, s1, m, ms);
+    }
+    if constexpr (MODE == MODE_DOWN) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) state[wrap_pos(base + c0 + k, nx)] = u0[k];
+    } else {
+        for (int u = 1; u < H; ++u) ks_warp4_level(p, u & 1, u * R, W - u * R, u0, u1, s0, s1, m, ms);
+        // as tile_export: sl[i] = row 0 cell i, sl[h + i] = row 1 cell R + i,
+        // sr[j] = row 0 cell h + j, sr[h + j] = row 1 cell h - R + j
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int c = c0 + k;
+            if (c < h) sl[c] = u0[k]; else sr[c - h] = u0[k];
+            if (c >= R && c < h + R) sl[h + c - R] = u1[k];
+            if (c >= h - R && c < W - R) sr[h + c - (h - R)] = u1[k];
+        }
+    }
+}
+
+template <typename T>
+cudaError_t launch_swept_ks_warp(const Params<T> &p, int mode, int phase, T *st, T *sl, int64_t nx, cudaStream_t s) {
+    const int64_t ntile = nx / kKsWarpTile;
+    const unsigned grid = (unsigned)((ntile + kKsWarpTilesPerBlock - 1) / kKsWarpTilesPerBlock);
+    const int threads = 32 * kKsWarpTilesPerBlock;
+    switch (mode) {
+    case MODE_UP: k_swept_ks_warp<T, MODE_UP><<<grid, threads, 0, s>>>(p, st, sl, phase); break;
+    case MODE_DIAMOND: k_swept_ks_warp<T, MODE_DIAMOND><<<grid, threads, 0, s>>>(p, st, sl, phase); break;
+    default: k_swept_ks_warp<T, MODE_DOWN><<<grid, threads, 0, s>>>(p, st, sl, phase); break;
+    }
+    return cudaGetLastError();
+}
+
 template <int P, typename T>
 cudaError_t launch_swept(const void *vp, int mode, int phase, void *state, void *slots, int64_t nx, int W,
                          int threads_req, cudaStream_t s) {
@@ -615,6 +730,9 @@ cudaError_t launch_swept(const void *vp, int mode, int phase, void *state, void 
     const Params<T> &p = *static_cast<const Params<T> *>(vp);
     const int threads = swept_threads_for<P, T>(W, threads_req);
     G *st = static_cast<G *>(state), *sl = static_cast<G *>(slots);
+    if constexpr (P == SW_KS && sizeof(T) == 4) {  // 128-cell tiles: one warp each, rows in registers
+        if (W == kKsWarpTile && threads == 32) return launch_swept_ks_warp<T>(p, mode, phase, st, sl, nx, s);
+    }
     if constexpr (P != SW_EULER) {
         if (threads * 4 == W) return launch_swept_path<P, T, PATH_SPAN4>(p, mode, phase, st, sl, nx, W, threads, s);
     }

@@ -222,3 +222,17 @@ def test_bounded_wait_reports_timeout(sw, solver, oracle):
     got, _ = _gpu(sw, solver, KS, 8, VARIANT, nx, 64, dt, 40, ic)
     _assert_identical(got, oracle.classic(c, ic, 40), "after the timeout")
     assert solver.wait_probe(10)[0] == -1  # limit out of range: SW_ERR_ARG, nothing launched
+
+
+@pytest.mark.parametrize("nx", [128, 256, 4096])
+def test_ks_fp32_warp_tiles(sw, solver, oracle, nx):
+    """FP32 KS swept at tile 128 runs each tile in one warp's registers: bit for
+    bit the oracle, for a single-tile domain (both halves wrap onto the same
+    tile), two tiles and many, over several diamond counts and remainders."""
+    dt = PROBLEM_DT[KS]
+    c = _case(oracle, KS, 4, nx, dt)
+    ic = _ic(oracle, KS, 4, nx, kind="random", seed=nx)
+    for nsteps in (16, 32, 33, 160, 321):
+        want = oracle.classic(c, ic, nsteps)
+        got, _ = _gpu(sw, solver, KS, 4, SWEPT, nx, 128, dt, nsteps, ic)
+        _assert_identical(got, want, "fp32 ks warp tiles nx %d steps %d" % (nx, nsteps))
