@@ -265,6 +265,108 @@ __device__ __forceinline__ bool ks_warp_tile(const Params<T> &p, T *__restrict__
 
 constexpr int kKsWarpNodesPerBlock = 8;
 
+// FP64 KS nodes: the same one-warp nodes through shared memory -- each warp
+// has its own tile rows and runs persistent_tile's steps with warp barriers,
+// using the block's shared tile code (tile_put / tile_point / tile_get), so
+// the results are those of persistent_tile bit for bit.  Eight nodes per block
+// lift the per-SM warp count above the 32 that one-warp blocks allow.
+template <typename T>
+__device__ __forceinline__ bool ks_smem_node_tile(const Params<T> &p, T *__restrict__ state, T *__restrict__ slots,
+                                                  unsigned *flags, int *status, T *rows, const int64_t q,
+                                                  const int64_t last, const int64_t t) {
+    constexpr int W = 32, h = 16, R = 2, H = W / (2 * R);
+    const int L = row_stride(W), x = threadIdx.x & 31;
+    const int64_t nx = p.nx, nhalf = nx / h;
+    const int phase = (int)(q & 1);
+    const int64_t base = t * W + (int64_t)phase * h;
+    const int64_t hl = (2 * t + phase) % nhalf;
+    const int64_t hr = (hl + 1 == nhalf) ? 0 : hl + 1;
+    T *sl = slots + hl * W, *sr = slots + hr * W;
+    if (q == 0) {
+        tile_put<SW_KS, T>(rows, L, 0, x, state[base + x]);
+    } else {
+        if (!wait_slots_warp(flags, hl, hr, (unsigned)q, status)) return false;
+        if (x < h) {  // as tile_import_cg, one cell per lane
+            tile_put<SW_KS, T>(rows, L, 0, x, ldcg(sl + x));
+            tile_put<SW_KS, T>(rows, L, 1, x - R, ldcg(sl + h + x));
+        } else {
+            const int j = x - h;
+            tile_put<SW_KS, T>(rows, L, 0, h + j, ldcg(sr + j));
+            tile_put<SW_KS, T>(rows, L, 1, h + R + j, ldcg(sr + h + j));
+        }
+    }
+    __syncwarp();
+    const Ends e{INT32_MIN / 2, INT32_MIN / 2};  // KS is periodic: no end cells
+    if (q > 0) {
+        for (int jl = 1; jl <= H; ++jl) {
+            if (x >= h - jl * R && x < h + jl * R) tile_point<SW_KS, T>(p, rows, L, jl & 1, x, e);
+            __syncwarp();
+        }
+    }
+    if (q == last) {
+        state[wrap_pos(base + x, nx)] = tile_get<SW_KS, T>(rows, L, 0, x);
+        return true;
+    }
+    for (int u = 1; u < H; ++u) {
+        if (x >= u * R && x < W - u * R) tile_point<SW_KS, T>(p, rows, L, u & 1, x, e);
+        __syncwarp();
+    }
+    if (x < h) {  // as tile_export
+        sl[x] = tile_get<SW_KS, T>(rows, L, 0, x);
+        sl[h + x] = tile_get<SW_KS, T>(rows, L, 1, R + x);
+    } else {
+        const int j = x - h;
+        sr[j] = tile_get<SW_KS, T>(rows, L, 0, h + j);
+        sr[h + j] = tile_get<SW_KS, T>(rows, L, 1, h - R + j);
+    }
+    __threadfence();
+    __syncwarp();
+    if (x == 0) {
+        st_release_u32(flags + hl, (unsigned)(q + 1));
+        st_release_u32(flags + hr, (unsigned)(q + 1));
+    }
+    __syncwarp();  // the next stage's import overwrites this warp's rows
+    return true;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(32 * kKsWarpNodesPerBlock)
+    k_persistent_ks_smem_nodes(const Params<T> p, T *__restrict__ state, T *__restrict__ slots,
+                               unsigned *__restrict__ flags, int *status, const int64_t n_diamonds) {
+    extern __shared__ __align__(16) unsigned char sw_smem[];
+    T *rows = reinterpret_cast<T *>(sw_smem) + (threadIdx.x >> 5) * (tile_rows<SW_KS>() * row_stride(32));
+    const int64_t ntile = p.nx / 32, last = n_diamonds + 1;
+    const int64_t w0 = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t q = 0; q <= last; ++q)
+        for (int64_t t = w0; t < ntile; t += nw)
+            if (!ks_smem_node_tile<T>(p, state, slots, flags, status, rows, q, last, t)) return;
+}
+
+template <typename T>
+cudaError_t launch_persistent_ks_smem_nodes(const Params<T> &p, T *st, T *sl, unsigned *flags, int *status,
+                                            int64_t nx, int64_t n_diamonds, cudaStream_t s) {
+    auto kern = k_persistent_ks_smem_nodes<T>;
+    const int threads = 32 * kKsWarpNodesPerBlock;
+    const size_t smem = kKsWarpNodesPerBlock * swept_smem_bytes<SW_KS, T>(32);
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) return cudaErrorInvalidConfiguration;
+    const int64_t ntile = nx / 32;
+    int64_t grid = (int64_t)per_sm * sms;
+    const int64_t need = (ntile + kKsWarpNodesPerBlock - 1) / kKsWarpNodesPerBlock;
+    if (grid > need) grid = need;
+    e = cudaMemsetAsync(flags, 0, sizeof(unsigned) * (nx / 16), s);
+    if (e != cudaSuccess) return e;
+    Params<T> pv = p;
+    int64_t nd = n_diamonds;
+    void *args[] = {&pv, &st, &sl, &flags, &status, &nd};
+    return cudaLaunchCooperativeKernel((const void *)kern, dim3((unsigned)grid), dim3(threads), args, smem, s);
+}
+
 template <typename T>
 __global__ void __launch_bounds__(32 * kKsWarpNodesPerBlock)
     k_persistent_ks_warp(const Params<T> p, T *__restrict__ state, T *__restrict__ slots, unsigned *__restrict__ flags,
@@ -404,6 +506,9 @@ cudaError_t launch_persistent(const void *vp, void *state, void *slots, unsigned
     // cover the FP64 latency (5.9e9 against 7.1e9), so FP64 keeps shared memory.
     if constexpr (P == SW_KS && sizeof(T) == 4) {
         if (W == 32) return launch_persistent_ks_warp<T>(p, st, sl, flags, status, nx, n_diamonds, s);
+    }
+    if constexpr (P == SW_KS && sizeof(T) == 8) {
+        if (W == 32) return launch_persistent_ks_smem_nodes<T>(p, st, sl, flags, status, nx, n_diamonds, s);
     }
     if (span4_launch<P, T>(W, threads))
         return launch_persistent_path<P, T, PATH_SPAN4>(p, st, sl, flags, status, nx, W, threads, n_diamonds, s);
