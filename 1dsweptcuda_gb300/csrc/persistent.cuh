@@ -152,16 +152,13 @@ __global__ void __launch_bounds__(Scheme<P, T>::MAXT)
             if (!persistent_tile<P, T, PATH>(p, state, slots, flags, status, rows, W, q, last, t)) return;
 }
 
-// ------------------------------------------------------- KS 32-cell warp nodes
-// KS alg 2 (the reference's register path, KS1D_SweptShared.cu:396-592): one
-// warp per 32-cell node and the node's rows in registers.  Lane x holds cell x
-// of row 0 (u) and row 1 (the predictor u*) and their squares; neighbours come
-// by shuffles.  Cells -2, -1, 32, 33 of row 1, which only the last down level
-// reads, sit in four more registers of every lane.  The slots, flags, stage
-// order and arithmetic (ks_*_sq) are those of persistent_tile with W = 32, so
-// the results are the same bit for bit; a block holds 8 nodes and no shared
-// memory, and no barrier wider than the warp.  Used for FP32 (see
-// launch_persistent).
+// ---------------------------------------------------------- KS 32-cell nodes
+// KS alg 2 (the reference's register path, KS1D_SweptShared.cu:396-592) runs
+// 32-cell nodes, one warp each, eight per block.  Each warp has its own tile
+// rows in shared memory and runs persistent_tile's steps with warp barriers
+// only, using the block's shared tile code (tile_put / tile_point / tile_get),
+// so the results are those of persistent_tile bit for bit.  Eight nodes per
+// block lift the per-SM warp count above the 32 that one-warp blocks allow.
 
 // Lane 0 waits as wait_slots does; the warp learns the outcome by a shuffle.
 __device__ __forceinline__ bool wait_slots_warp(const unsigned *flags, int64_t hl, int64_t hr, unsigned need,
@@ -185,91 +182,8 @@ __device__ __forceinline__ bool wait_slots_warp(const unsigned *flags, int64_t h
     return good != 0;
 }
 
-// One sub-step of parity `par` on node cells [lo, hi): lane x updates cell x
-// when it lies in the range.  `m`/`ms` are the row-1 margin cells -2, -1, 32, 33
-// and their squares (used when the source is row 1, par = 0).
-template <typename T>
-__device__ __forceinline__ void ks_warp_level(const Params<T> &p, int par, int lo, int hi, T &u0, T &u1, T &s0, T &s1,
-                                              const T (&m)[4], const T (&ms)[4]) {
-    const unsigned full = 0xffffffffu;
-    const int lane = threadIdx.x & 31;
-    const T src = par ? u0 : u1, sq = par ? s0 : s1;
-    T a = __shfl_up_sync(full, src, 2), b = __shfl_up_sync(full, src, 1);
-    T d = __shfl_down_sync(full, src, 1), e = __shfl_down_sync(full, src, 2);
-    T bs = __shfl_up_sync(full, sq, 1), ds = __shfl_down_sync(full, sq, 1);
-    if (!par) {  // cells -2, -1 and 32, 33 of row 1
-        if (lane == 0) { a = m[0]; b = m[1]; bs = ms[1]; }
-        if (lane == 1) a = m[1];
-        if (lane == 30) e = m[2];
-        if (lane == 31) { d = m[2]; e = m[3]; ds = ms[2]; }
-    }
-    const T v = par ? ks_predict_sq(p, a, b, src, d, e, bs, ds) : ks_correct_sq(p, u0, a, b, src, d, e, bs, ds);
-    const T v2 = ml(v, v);
-    if (lane >= lo && lane < hi) {
-        if (par) { u1 = v; s1 = v2; } else { u0 = v; s0 = v2; }
-    }
-}
-
-// Stage q of node t (persistent_tile for KS, W = 32, in one warp).
-template <typename T>
-__device__ __forceinline__ bool ks_warp_tile(const Params<T> &p, T *__restrict__ state, T *__restrict__ slots,
-                                             unsigned *flags, int *status, const int64_t q, const int64_t last,
-                                             const int64_t t) {
-    constexpr int W = 32, h = 16, R = 2;
-    const int lane = threadIdx.x & 31;
-    const int64_t nx = p.nx, nhalf = nx / h;
-    const int phase = (int)(q & 1);
-    const int64_t base = t * W + (int64_t)phase * h;
-    const int64_t hl = (2 * t + phase) % nhalf;
-    const int64_t hr = (hl + 1 == nhalf) ? 0 : hl + 1;
-    T u0, u1 = T(0), m[4] = {T(0), T(0), T(0), T(0)};
-    if (q == 0) {
-        u0 = state[base + lane];
-    } else {
-        if (!wait_slots_warp(flags, hl, hr, (unsigned)q, status)) return false;
-        const T *sl = slots + hl * W, *sr = slots + hr * W;
-        // slot layout as tile_import: sl = [row 0, cells 0..15][row 1, cells -2..13],
-        // sr = [row 0, cells 16..31][row 1, cells 18..33]
-        u0 = lane < h ? ldcg(sl + lane) : ldcg(sr + lane - h);
-        if (lane < h - R) u1 = ldcg(sl + h + lane + R);
-        else if (lane >= h + R) u1 = ldcg(sr + lane - R);
-        m[0] = ldcg(sl + h);
-        m[1] = ldcg(sl + h + 1);
-        m[2] = ldcg(sr + W - 2);
-        m[3] = ldcg(sr + W - 1);
-    }
-    T s0 = ml(u0, u0), s1 = ml(u1, u1);
-    const T ms[4] = {ml(m[0], m[0]), ml(m[1], m[1]), ml(m[2], m[2]), ml(m[3], m[3])};
-    if (q > 0) {
-        for (int j = 1; j <= h / R; ++j) ks_warp_level(p, j & 1, h - j * R, h + j * R, u0, u1, s0, s1, m, ms);
-    }
-    if (q == last) {
-        state[wrap_pos(base + lane, nx)] = u0;
-        return true;
-    }
-    for (int u = 1; u < h / R; ++u) ks_warp_level(p, u & 1, u * R, W - u * R, u0, u1, s0, s1, m, ms);
-    T *sl = slots + hl * W, *sr = slots + hr * W;
-    // as tile_export: sl[i] = row 0 cell i, sl[h + i] = row 1 cell R + i;
-    // sr[j] = row 0 cell h + j, sr[h + j] = row 1 cell h - R + j
-    if (lane < h) sl[lane] = u0; else sr[lane - h] = u0;
-    if (lane >= R && lane < h + R) sl[h + lane - R] = u1;
-    if (lane >= h - R && lane < W - R) sr[h + lane - (h - R)] = u1;
-    __threadfence();
-    __syncwarp();
-    if (lane == 0) {
-        st_release_u32(flags + hl, (unsigned)(q + 1));
-        st_release_u32(flags + hr, (unsigned)(q + 1));
-    }
-    return true;
-}
-
 constexpr int kKsWarpNodesPerBlock = 8;
 
-// FP64 KS nodes: the same one-warp nodes through shared memory -- each warp
-// has its own tile rows and runs persistent_tile's steps with warp barriers,
-// using the block's shared tile code (tile_put / tile_point / tile_get), so
-// the results are those of persistent_tile bit for bit.  Eight nodes per block
-// lift the per-SM warp count above the 32 that one-warp blocks allow.
 template <typename T>
 __device__ __forceinline__ bool ks_smem_node_tile(const Params<T> &p, T *__restrict__ state, T *__restrict__ slots,
                                                   unsigned *flags, int *status, T *rows, const int64_t q,
@@ -365,41 +279,6 @@ cudaError_t launch_persistent_ks_smem_nodes(const Params<T> &p, T *st, T *sl, un
     int64_t nd = n_diamonds;
     void *args[] = {&pv, &st, &sl, &flags, &status, &nd};
     return cudaLaunchCooperativeKernel((const void *)kern, dim3((unsigned)grid), dim3(threads), args, smem, s);
-}
-
-template <typename T>
-__global__ void __launch_bounds__(32 * kKsWarpNodesPerBlock)
-    k_persistent_ks_warp(const Params<T> p, T *__restrict__ state, T *__restrict__ slots, unsigned *__restrict__ flags,
-                         int *status, const int64_t n_diamonds) {
-    const int64_t ntile = p.nx / 32, last = n_diamonds + 1;
-    const int64_t w0 = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
-    for (int64_t q = 0; q <= last; ++q)
-        for (int64_t t = w0; t < ntile; t += nw)
-            if (!ks_warp_tile<T>(p, state, slots, flags, status, q, last, t)) return;
-}
-
-template <typename T>
-cudaError_t launch_persistent_ks_warp(const Params<T> &p, T *st, T *sl, unsigned *flags, int *status, int64_t nx,
-                                      int64_t n_diamonds, cudaStream_t s) {
-    auto kern = k_persistent_ks_warp<T>;
-    const int threads = 32 * kKsWarpNodesPerBlock;
-    int dev = 0, sms = 0, per_sm = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, 0);
-    if (e != cudaSuccess) return e;
-    if (per_sm < 1) return cudaErrorInvalidConfiguration;
-    const int64_t ntile = nx / 32;
-    int64_t grid = (int64_t)per_sm * sms;
-    const int64_t need = (ntile + kKsWarpNodesPerBlock - 1) / kKsWarpNodesPerBlock;
-    if (grid > need) grid = need;
-    e = cudaMemsetAsync(flags, 0, sizeof(unsigned) * (nx / 16), s);
-    if (e != cudaSuccess) return e;
-    Params<T> pv = p;
-    int64_t nd = n_diamonds;
-    void *args[] = {&pv, &st, &sl, &flags, &status, &nd};
-    return cudaLaunchCooperativeKernel((const void *)kern, dim3((unsigned)grid), dim3(threads), args, 0, s);
 }
 
 // ------------------------------------------------------------ ensembles
@@ -500,14 +379,7 @@ cudaError_t launch_persistent(const void *vp, void *state, void *slots, unsigned
     const Params<T> &p = *static_cast<const Params<T> *>(vp);
     const int threads = swept_threads_for<P, T>(W, threads_req);
     G *st = static_cast<G *>(state), *sl = static_cast<G *>(slots);
-    // FP32 KS nodes run in warp registers (1.47e11 against 9.6e10 cell-updates/s
-    // through shared memory at nx = 2^22).  In FP64 the register version's 66
-    // registers leave 24 warps per SM against 32 one-warp blocks, too few to
-    // cover the FP64 latency (5.9e9 against 7.1e9), so FP64 keeps shared memory.
-    if constexpr (P == SW_KS && sizeof(T) == 4) {
-        if (W == 32) return launch_persistent_ks_warp<T>(p, st, sl, flags, status, nx, n_diamonds, s);
-    }
-    if constexpr (P == SW_KS && sizeof(T) == 8) {
+    if constexpr (P == SW_KS) {
         if (W == 32) return launch_persistent_ks_smem_nodes<T>(p, st, sl, flags, status, nx, n_diamonds, s);
     }
     if (span4_launch<P, T>(W, threads))
