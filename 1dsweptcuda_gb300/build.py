@@ -29,7 +29,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # operation with a round-to-nearest intrinsic, so they never depend on it.
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC",
                      "-Xptxas", "-warn-spills", "-I", str(INCLUDE)]
-CU_SOURCES = ["k_heat.cu", "k_ks.cu", "k_euler.cu", "api.cu", "batch.cu", "noalloc.cu", "closure.cu", "diag.cu"]
+CU_SOURCES = ["k_heat.cu", "k_ks.cu", "k_ks_div.cu", "k_euler.cu", "api.cu", "batch.cu", "noalloc.cu", "closure.cu", "diag.cu"]
 CPP_SOURCES = ["cli.cpp"]
 HEADERS = ["engine.cuh", "stencils.cuh", "persistent.cuh", "sw_internal.h", "ctx.h"]
 PROGRAMS = [(p, pi, q, qi) for pi, p in enumerate(("Heat", "KS", "Euler")) for q, qi in (("Single", 4), ("Double", 8))]
@@ -65,7 +65,8 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     for src in CU_SOURCES:
         o = OBJ / (src + ".o")
         objs.append(o)
-        if force or _stale(o, [CSRC / src] + hdrs):
+        deps = [CSRC / src] + ([CSRC / "k_ks.cu"] if src == "k_ks_div.cu" else []) + hdrs  # k_ks_div.cu includes k_ks.cu
+        if force or _stale(o, deps):
             jobs.append(["nvcc", "-c", str(CSRC / src), "-o", str(o)] + NVCC_FLAGS)
     for src in CPP_SOURCES:
         o = OBJ / (src + ".o")

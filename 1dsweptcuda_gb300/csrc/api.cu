@@ -42,9 +42,16 @@ void derive(const sw_config &c, sw_constants &k) {
     } else if (c.problem == SW_KS) {
         // KS1D_SweptShared.cu:45,887,917-926
         const R dx = (R)(c.dx != 0 ? c.dx : 0.5);
-        k.dx_times4 = R(1) / (R(4) * dx);
-        k.dx2 = R(1) / (dx * dx);
-        k.dx4 = R(1) / (dx * dx * dx * dx);
+        if (c.flags & SW_FLAG_KS_DIVIDE) {
+            // the DIVISE build's divisors, KS1D_SweptShared.cu:904-914
+            k.dx_times4 = R(4) * dx;
+            k.dx2 = dx * dx;
+            k.dx4 = dx * dx * dx * dx;
+        } else {
+            k.dx_times4 = R(1) / (R(4) * dx);
+            k.dx2 = R(1) / (dx * dx);
+            k.dx4 = R(1) / (dx * dx * dx * dx);
+        }
         k.dt = (R)c.dt;
         k.dt_half = (R)(c.dt * 0.5);
         k.lx = (double)((R)nx * dx);
@@ -294,7 +301,7 @@ int ensure_buffers(sw_ctx *ctx, const sw_config &c, const Ops *ops, bool need_io
 template <typename T>
 int run_impl(sw_ctx *ctx, const sw_config &c, const void *ic_host, void *final_host, void *state_dev,
              cudaStream_t stream, sw_snapshot_fn cb, void *user, sw_result *out) {
-    const Ops *ops = ops_for(c.problem, c.precision);
+    const Ops *ops = ops_for(c.problem, c.precision, c.flags);
     if (!ops) return fail(ctx, SW_ERR_ARG, "unknown problem/precision");
     sw_constants k;
     derive<T>(c, k);
@@ -485,6 +492,8 @@ int sw_validate(const sw_config *c) {
     if (c->alg < SW_ALG_CLASSIC || c->alg > SW_ALG_SELFTEST) return SW_ERR_ARG;
     if (c->alg == SW_ALG_SELFTEST && c->problem != SW_KS) return SW_ERR_ARG;
     if (c->time_mode != SW_TIME_REFERENCE && c->time_mode != SW_TIME_STEPS) return SW_ERR_ARG;
+    if ((c->flags & ~SW_FLAG_KS_DIVIDE) != 0) return SW_ERR_ARG;
+    if ((c->flags & SW_FLAG_KS_DIVIDE) && c->problem != SW_KS) return SW_ERR_ARG;
     const int bc = resolved_bc(*c);
     if (c->problem == SW_HEAT && bc != SW_BC_MIRROR && bc != SW_BC_PERIODIC) return SW_ERR_ARG;
     if (c->problem == SW_KS && bc != SW_BC_PERIODIC) return SW_ERR_ARG;
@@ -574,7 +583,7 @@ int sw_plan(const sw_config *cfg, sw_plan_info *out, double *snap_t, int64_t *sn
     int rc = sw_validate(cfg);
     if (rc) return rc;
     if (cfg->alg == SW_ALG_SELFTEST) return SW_ERR_UNSUPPORTED;
-    const Ops *ops = ops_for(cfg->problem, cfg->precision);
+    const Ops *ops = ops_for(cfg->problem, cfg->precision, cfg->flags);
     if (!ops) return SW_ERR_ARG;
     const int W = tile_width(*cfg);
     Plan pl = (cfg->time_mode == SW_TIME_STEPS) ? plan_steps(*cfg, W, ops->R, ops->S)

@@ -137,7 +137,7 @@ bool same_key(const GraphKey &a, const GraphKey &b) { return std::memcmp(&a, &b,
 template <typename T>
 int run_batch_device(sw_ctx *ctx, const sw_config &c0, int32_t n, const int64_t *nx, void *state, cudaStream_t user,
                      sw_result *out, bool tuning_pass, double *ms_out) {
-    const Ops *ops = ops_for(c0.problem, c0.precision);
+    const Ops *ops = ops_for(c0.problem, c0.precision, c0.flags);
     sw_config c = c0;
     if (c.alg != SW_ALG_CLASSIC && c.tpb == 0) {
         sw_tuning t;
@@ -260,7 +260,7 @@ int sw_run_batch(sw_ctx *ctx, const sw_config *cfg, int32_t n, const int64_t *nx
     int rc = check_batch(cfg, n, nx);
     if (rc) return fail(ctx, rc, std::string("invalid ensemble: ") + sw_strerror(rc));
     if (!ic_host || !final_host) return fail(ctx, SW_ERR_ARG, "sw_run_batch needs ic_host and final_host");
-    const Ops *ops = ops_for(cfg->problem, cfg->precision);
+    const Ops *ops = ops_for(cfg->problem, cfg->precision, cfg->flags);
     int64_t cells = 0;
     for (int32_t d = 0; d < n; ++d) cells += nx[d];
     SW_CUDA(ctx, cudaSetDevice(ctx->device));
@@ -300,7 +300,7 @@ int sw_query_tuning(sw_ctx *ctx, const sw_config *cfg, int32_t n, const int64_t 
     }
     std::memset(out, 0, sizeof(*out));
     if (c.alg == SW_ALG_CLASSIC) return SW_OK;
-    const Ops *ops = ops_for(c.problem, c.precision);
+    const Ops *ops = ops_for(c.problem, c.precision, c.flags);
     // sample: every k-th domain, at least kTuneCells cells where the ensemble has that many
     int64_t total = 0;
     for (int32_t d = 0; d < n; ++d) total += nx[d];

@@ -282,6 +282,12 @@ int cli(int problem, int argc, char **argv) {
     cfg.freq = std::atof(argv[5]);
     cfg.alg = std::atoi(argv[6]);
     cfg.time_mode = SW_TIME_REFERENCE;
+    // The reference chooses its KS division form when it is compiled (-DDIVISE,
+    // KS1D_SweptShared.cu:111,904); these programs take it from the environment.
+    if (problem == SW_KS) {
+        const char *d = std::getenv("SWEPT1D_KS_DIVIDE");
+        if (d && *d && std::strcmp(d, "0") != 0) cfg.flags |= SW_FLAG_KS_DIVIDE;
+    }
     std::cout.precision(10);
 
     sw_constants k;

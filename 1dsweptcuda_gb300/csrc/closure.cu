@@ -519,6 +519,7 @@ int sw_closure_step(sw_ctx *ctx, const sw_config *coarse, const float *theta, fl
     if (rc) return rc;
     if (!coarse || !u || (use_closure && !theta)) return SW_ERR_ARG;
     if (coarse->problem != SW_KS || coarse->precision != 4) return fail(ctx, SW_ERR_UNSUPPORTED, "closure steps KS FP32");
+    if (coarse->flags != 0) return fail(ctx, SW_ERR_UNSUPPORTED, "closure steps take no sw_config.flags");
     sw_config c = *coarse;
     c.nx = n;
     sw_constants k;

@@ -82,7 +82,9 @@ inline Params<T> make_params(const sw_config &c, const sw_constants &k) {
         int e = 0;
         return v > T(0) && std::isfinite((double)v) && std::frexp((double)v, &e) == 0.5;
     };
-    p.pow2 = (c.problem == SW_KS && is_pow2(p.c4) && is_pow2(p.d2) && is_pow2(p.d4)) ? 1 : 0;
+    if (c.problem == SW_KS && (c.flags & SW_FLAG_KS_DIVIDE)) p.ks_form = KS_DIVIDE;
+    else if (c.problem == SW_KS && is_pow2(p.c4) && is_pow2(p.d2) && is_pow2(p.d4)) p.ks_form = KS_POW2;
+    else p.ks_form = KS_MULTIPLY;
     return p;
 }
 

@@ -36,7 +36,7 @@
 #include "stencils.cuh"
 #include "sw_internal.h"
 
-namespace sw {
+SW_KERNELS_BEGIN
 
 template <typename T>
 struct alignas(4 * sizeof(T)) V4 {
@@ -757,4 +757,4 @@ size_t smem_of(int W) {
     return swept_smem_bytes<P, T>(W);
 }
 
-}  // namespace sw
+SW_KERNELS_END

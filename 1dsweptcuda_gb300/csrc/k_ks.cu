@@ -28,7 +28,11 @@ Ops make_ops() {
 }
 }  // namespace
 
+#ifdef SW_KS_DIVIDE_TU
+const Ops *ks_divide_ops(int prec) {
+#else
 const Ops *ks_ops(int prec) {
+#endif
     static const Ops f = make_ops<float>();
     static const Ops d = make_ops<double>();
     return prec == 4 ? &f : (prec == 8 ? &d : nullptr);

@@ -45,7 +45,7 @@ cudaError_t scratch_address(void **out) {
 
 template <typename T>
 int run(const sw_config &c, void *state, cudaStream_t s) {
-    const Ops *ops = ops_for(c.problem, c.precision);
+    const Ops *ops = ops_for(c.problem, c.precision, c.flags);
     const int W = c.tpb;
     const int64_t nx = c.nx;
     const size_t slot_bytes = ops->cell * (size_t)nx * 2;

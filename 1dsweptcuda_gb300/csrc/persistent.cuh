@@ -24,7 +24,7 @@
 #define SW_WAIT_NS 4000000000ull  // 4 s per wait
 #endif
 
-namespace sw {
+SW_KERNELS_BEGIN
 
 __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
     unsigned v;
@@ -480,4 +480,4 @@ cudaError_t launch_persistent_batch(const void *vp, void *state, void *slots, co
     return launch_persistent_batch_path<P, T, PATH_CELL>(p, st, sl, b, flags, status, W, threads, n_diamonds, s);
 }
 
-}  // namespace sw
+SW_KERNELS_END

@@ -11,7 +11,21 @@
 
 #include "sw_internal.h"
 
-namespace sw {
+// k_ks_div.cu compiles the kernel headers (this file, engine.cuh,
+// persistent.cuh) a second time with SW_KS_DIVIDE_TU defined: the KS
+// right-hand side then divides (SW_FLAG_KS_DIVIDE), and every template
+// instance of that build lands in the inline namespace sw::ks_divide, apart
+// from the default build's.  The default build's kernels never carry the
+// divisions, so its register allocation is the same as without them.
+#ifdef SW_KS_DIVIDE_TU
+#define SW_KERNELS_BEGIN namespace sw { inline namespace ks_divide {
+#define SW_KERNELS_END } }
+#else
+#define SW_KERNELS_BEGIN namespace sw {
+#define SW_KERNELS_END }
+#endif
+
+SW_KERNELS_BEGIN
 
 // ---- correctly rounded scalar operations, both precisions
 __device__ __forceinline__ double ad(double a, double b) { return __dadd_rn(a, b); }
@@ -45,17 +59,23 @@ __device__ __forceinline__ T heat_step(const Params<T> &p, T l, T c, T r) {
 // A product by an exact power of two is exact, so folding it into the
 // following add as one fused multiply-add rounds exactly as the separate
 // multiply and add do.  That holds for the literal 2 and 4 always, and for the
-// reciprocals c4, d2, d4 when they are powers of two (p.pow2, set by the host:
+// reciprocals c4, d2, d4 when they are powers of two (KS_POW2, set by the host:
 // 0.5, 4, 16 at the reference's dx = 0.5).  Results stay bit-identical to the
 // reference's expression while the FP64 pipe does 15 operations instead of 20
 // (barring overflow or underflow of the scaled terms, ~1e+-300).
+// KS_DIVIDE is the DIVISE build (KS1D_SweptShared.cu:111-132): each term divided
+// by 4dx, dx^2, dx^4, summed in the same order.
 template <typename T>
 __device__ __forceinline__ T ks_rhs_sq(const Params<T> &p, T ll, T l, T c, T r, T rr, T l2, T r2) {
     const T conv = sb(r2, l2);  // l2 = l*l, r2 = r*r
     const T sec = fm(T(-2), c, ad(l, r));                        // (l + r) - 2c
     const T fourth = ad(fm(T(-4), r, ad(fm(T(-4), l, ll), ml(T(6), c))), rr);  // ((ll - 4l) + 6c) - 4r + rr
-    if (p.pow2) return fm(fourth, p.d4, fm(conv, p.c4, ml(sec, p.d2)));
+#ifdef SW_KS_DIVIDE_TU
+    return ad(ad(dv(conv, p.c4), dv(sec, p.d2)), dv(fourth, p.d4));
+#else
+    if (p.ks_form == KS_POW2) return fm(fourth, p.d4, fm(conv, p.c4, ml(sec, p.d2)));
     return ad(ad(ml(conv, p.c4), ml(sec, p.d2)), ml(fourth, p.d4));
+#endif
 }
 template <typename T>
 __device__ __forceinline__ T ks_rhs(const Params<T> &p, T ll, T l, T c, T r, T rr) {
@@ -212,4 +232,4 @@ __device__ __forceinline__ Q3<T> eu_correct(const Params<T> &p, Q3<T> u, const Q
     return qadd(u, qscale(ml(T(0.5), p.dtdx), f));
 }
 
-}  // namespace sw
+SW_KERNELS_END

@@ -20,8 +20,13 @@ struct Params {
     T bd[6];                   // Euler boundary states (rho, rho u, E) left, right
     int64_t nx;
     int bc;                    // SW_BC_MIRROR / PERIODIC / DIRICHLET
-    int pow2;                  // KS: c4, d2, d4 are exact powers of two (products by them are exact)
+    int ks_form;               // KS: how c4, d2, d4 enter the right-hand side (enum KsForm)
 };
+
+// KS right-hand-side forms.  KS_POW2: c4, d2, d4 are exact powers of two, so
+// their products fold into fused multiply-adds without changing a bit;
+// KS_DIVIDE: c4, d2, d4 are the divisors 4dx, dx^2, dx^4 (SW_FLAG_KS_DIVIDE).
+enum KsForm { KS_MULTIPLY = 0, KS_POW2 = 1, KS_DIVIDE = 2 };
 
 // Device tables of an ensemble (see sw_run_batch): domain d holds cells
 // [off[d], off[d+1]), its slots are the same range times two, its flags
@@ -77,12 +82,13 @@ struct Ops {
 
 const Ops *heat_ops(int prec);
 const Ops *ks_ops(int prec);
+const Ops *ks_divide_ops(int prec);  // SW_FLAG_KS_DIVIDE (k_ks_div.cu)
 const Ops *euler_ops(int prec);
 
-inline const Ops *ops_for(int problem, int prec) {
+inline const Ops *ops_for(int problem, int prec, int flags) {
     switch (problem) {
     case SW_HEAT: return heat_ops(prec);
-    case SW_KS: return ks_ops(prec);
+    case SW_KS: return (flags & SW_FLAG_KS_DIVIDE) ? ks_divide_ops(prec) : ks_ops(prec);
     case SW_EULER: return euler_ops(prec);
     default: return nullptr;
     }

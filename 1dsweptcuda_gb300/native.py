@@ -18,6 +18,7 @@ HEAT, KS, EULER = 0, 1, 2
 ALG_CLASSIC, ALG_SWEPT, ALG_VARIANT, ALG_SELFTEST = 0, 1, 2, 3
 BC_DEFAULT, BC_MIRROR, BC_PERIODIC, BC_DIRICHLET = 0, 1, 2, 3
 TIME_REFERENCE, TIME_STEPS = 0, 1
+FLAG_KS_DIVIDE = 1  # sw_config.flags: KS divides by 4dx, dx^2, dx^4 (the reference's DIVISE build)
 COMPONENTS = {HEAT: 1, KS: 1, EULER: 3}
 PROBLEM_NAMES = {HEAT: "Heat", KS: "KS", EULER: "Euler"}
 
@@ -41,7 +42,7 @@ class Config(C.Structure):
         ("dt", C.c_double), ("tf", C.c_double), ("freq", C.c_double), ("n_steps", C.c_int64),
         ("dx", C.c_double), ("alpha", C.c_double), ("gamma", C.c_double),
         ("left", C.c_double * 3), ("right", C.c_double * 3),
-        ("threads", C.c_int32), ("reserved", C.c_int32),
+        ("threads", C.c_int32), ("flags", C.c_int32),
     ]
 
 

@@ -4,6 +4,7 @@ state resident on the device, and check that all paths agree bit for bit.
 
     python 1dsweptcuda_gb300/perf.py [--quick] [--ensemble] [--only TEXT] [--precision 4|8]
                                      [--threads 0,64,...] [--tpb 256,...] [--algs swept,...] [--json out.json]
+    python 1dsweptcuda_gb300/perf.py --divide [Divides.txt]     # the KS division study alone
 
 Each case runs SW_TIME_STEPS with a step count that is a whole number of swept
 cycles for every tpb in the case, timed with CUDA events inside the library
@@ -77,6 +78,48 @@ def ensemble_rows(sw, solver, quick: bool):
     return rows
 
 
+def divide_rows(sw, solver, quick: bool, path: str | None):
+    """The reference's division study (its Divides.txt: KS time per step with the
+    DIVISE build against the reciprocal build, FP64 and FP32, nx = 2^11..2^20):
+    KS swept, tpb = 256, dx = 0.5, dt = 0.005, SW_FLAG_KS_DIVIDE on and off.  At
+    dx = 0.5 both forms must give the same bits.  Writes the table in the study's
+    column order (nx, us/step divide FP64, multiply FP64, divide FP32, multiply
+    FP32) when a path is given."""
+    import numpy as np
+    import torch
+    stream = torch.cuda.current_stream()
+    rows, table = [], []
+    for e in range(11, 17 if quick else 21):
+        nx = 1 << e
+        steps = 4096
+        line = [nx]
+        for prec in (8, 4):
+            outs = []
+            for flags in (sw.FLAG_KS_DIVIDE, 0):
+                cfg = sw.make_config(sw.KS, prec, alg=sw.ALG_SWEPT, nx=nx, tpb=256, dt=0.005, flags=flags,
+                                     time_mode=sw.TIME_STEPS, n_steps=steps)
+                ic = sw.initial_condition(cfg)
+                st = torch.from_numpy(ic).cuda()
+                solver.run_device(cfg, st.data_ptr(), stream.cuda_stream)  # warm
+                st = torch.from_numpy(ic).cuda()
+                torch.cuda.synchronize()
+                res = solver.run_device(cfg, st.data_ptr(), stream.cuda_stream)
+                outs.append(st.cpu().numpy())
+                us = res.kernel_ms * 1e3 / steps
+                line.append(us)
+                rows.append({"case": "ks divide study nx=2^%d" % e, "precision": prec,
+                             "form": "divide" if flags else "multiply", "nx": nx, "steps": steps,
+                             "us_per_step": us, "cell_updates_per_s": nx * steps / (res.kernel_ms * 1e-3)})
+            rows[-2]["equal_to_multiply"] = bool(np.array_equal(outs[0], outs[1]))
+            print("ks divide study nx=2^%-2d f%-2d divide %9.3f us/step  multiply %9.3f us/step  x%.2f  %s" % (
+                e, prec * 8, line[-2], line[-1], line[-2] / line[-1],
+                "bit-identical" if rows[-2]["equal_to_multiply"] else "DIFFERS"), flush=True)
+        table.append(line)
+    if path:
+        Path(path).write_text("".join("%d\t%g\t%g\t%g\t%g\n" % tuple(t) for t in table))
+    return rows
+
+
 def main():
     import numpy as np
     import torch
@@ -90,6 +133,8 @@ def main():
     ap.add_argument("--threads", default="0", help="comma-separated threads per swept block (0 = default)")
     ap.add_argument("--tpb", default=None, help="comma-separated tile widths (default: each case's own)")
     ap.add_argument("--algs", default="classic,swept,variant", help="comma-separated subset of classic,swept,variant")
+    ap.add_argument("--divide", nargs="?", const="", default=None, metavar="TABLE",
+                    help="run only the KS division study; write its table to TABLE if given")
     args = ap.parse_args()
     sw = importlib.import_module("1dsweptcuda_gb300")
     solver = sw.Solver(0)
@@ -98,6 +143,12 @@ def main():
     algs = {"classic": sw.ALG_CLASSIC, "swept": sw.ALG_SWEPT, "variant": sw.ALG_VARIANT}
     alg_list = [algs[a] for a in args.algs.split(",")]
     rows = []
+    if args.divide is not None:
+        rows = divide_rows(sw, solver, args.quick, args.divide or None)
+        solver.close()
+        if args.json:
+            Path(args.json).write_text(json.dumps(rows, indent=1))
+        return
     for label, prob, prec, bc, nx, tpbs, steps, dt in cases(args.quick):
         if (args.only and not any(o in label for o in args.only.split(","))) or \
                 (args.precision and args.precision != prec):

@@ -72,6 +72,15 @@ enum sw_time_mode {
     SW_TIME_STEPS = 1      /* exactly n_steps time steps (swept finishes the remainder classically) */
 };
 
+/* sw_config.flags */
+enum sw_flag {
+    /* KS: divide by 4 dx, dx^2 and dx^4 instead of multiplying by their
+     * reciprocals -- the reference's DIVISE build (KS1D_SweptShared.cu:111-132,
+     * 904-914), kept for its divide-vs-multiply timing study.  At a power-of-two
+     * dx (the reference's 0.5) both forms give the same bits. */
+    SW_FLAG_KS_DIVIDE = 1
+};
+
 /* ------------------------------------------------------------ run config */
 typedef struct sw_config {
     int32_t problem;     /* enum sw_problem */
@@ -93,7 +102,7 @@ typedef struct sw_config {
     double right[3];     /* Euler right state (rho, u, p); all 0 = Sod (0.125, 0, 0.1) */
     int32_t threads;     /* threads per swept block: 0 = the library's default for the tile width; a
                             multiple of 32 up to min(tpb, 512) (Euler 256), else the default */
-    int32_t reserved;
+    int32_t flags;       /* enum sw_flag bits; 0 = none */
 } sw_config;
 
 /* Derived constants, rounded to the run's precision exactly as the
@@ -101,7 +110,7 @@ typedef struct sw_config {
  * KS1D_SweptShared.cu:917-926, Euler1D_SweptShared.cu:1127-1154). */
 typedef struct sw_constants {
     double fourier, fourier_two;                  /* Heat */
-    double dx_times4, dx2, dx4, dt, dt_half;      /* KS (reciprocals) */
+    double dx_times4, dx2, dx4, dt, dt_half;      /* KS (reciprocals; the divisors under SW_FLAG_KS_DIVIDE) */
     double gam, mgam, dt_dx;                      /* Euler */
     double bd[6];                                 /* Euler boundary states (rho, rho u, E) x 2 */
     double lx, dx;                                /* domain length and spacing as the .dat header prints them */

@@ -31,7 +31,7 @@ class Consts(C.Structure):
         ("dx_times4", C.c_double), ("dx2", C.c_double), ("dx4", C.c_double),
         ("dt", C.c_double), ("dt_half", C.c_double),
         ("gam", C.c_double), ("mgam", C.c_double), ("dt_dx", C.c_double),
-        ("bd", C.c_double * 6),
+        ("bd", C.c_double * 6), ("divide", C.c_int),
     ]
 
     def as_dict(self):
@@ -86,6 +86,22 @@ def reference_consts(problem: int, prec: int, nx: int, dt: float) -> Consts:
     c = Consts()
     if lib().or_reference_consts(problem, prec, nx, dt, C.byref(c)):
         raise ValueError("bad constants request")
+    return c
+
+
+def ks_consts(prec: int, nx: int, dt: float, dx: float = 0.5, divide: bool = False) -> Consts:
+    """KS constants at a given dx, rounded through REAL as main() rounds them:
+    the reciprocals 1/(4dx), 1/dx^2, 1/dx^4 (KS1D_SweptShared.cu:917-926), or
+    with ``divide`` the DIVISE build's divisors 4dx, dx^2, dx^4 (:904-914)."""
+    c = reference_consts(KS, prec, nx, dt)
+    R = np.float64 if prec == 8 else np.float32
+    d = R(dx)
+    if divide:
+        c4, d2, d4 = R(4) * d, d * d, d * d * d * d
+    else:
+        c4, d2, d4 = R(1) / (R(4) * d), R(1) / (d * d), R(1) / (d * d * d * d)
+    c.dx_times4, c.dx2, c.dx4 = float(c4), float(d2), float(d4)
+    c.divide = 1 if divide else 0
     return c
 
 

@@ -48,6 +48,9 @@ typedef struct or_consts {
     /* Euler (dimensions + dbd, Euler1D_SweptShared.cu:73-93) */
     double gam, mgam, dt_dx;
     double bd[6]; /* left (rho, rho u, E), right (rho, rho u, E) */
+    /* KS: 1 = the DIVISE build (KS1D_SweptShared.cu:111-132, 904-914):
+     * dx_times4, dx2, dx4 hold 4dx, dx^2, dx^4 and the terms are divided */
+    int divide;
 } or_consts;
 
 /* Advance `nsteps` full time steps of the classic scheme in place.

@@ -20,14 +20,21 @@ static inline REAL FN(heat_exec)(REAL fo, REAL fo2, REAL l, REAL c, REAL r)
 }
 
 /* ------------------------------------------------------------------- KS */
-/* convect / secondDer / fourthDer (multiply-by-reciprocal build),
- * KS1D_SweptShared.cu:136-155 */
+/* convect / secondDer / fourthDer: multiply-by-reciprocal build,
+ * KS1D_SweptShared.cu:136-155, or the DIVISE build, :111-132 (k->divide) */
 static inline REAL FN(ks_sum)(const or_consts *k, REAL ll, REAL l, REAL c, REAL r, REAL rr)
 {
     const REAL c4 = (REAL)k->dx_times4, d2 = (REAL)k->dx2, d4 = (REAL)k->dx4;
-    REAL conv = (r * r - l * l) * c4;
-    REAL sec = (l + r - (REAL)2 * c) * d2;
-    REAL four = (ll - (REAL)4 * l + (REAL)6 * c - (REAL)4 * r + rr) * d4;
+    REAL conv, sec, four;
+    if (k->divide) {
+        conv = (r * r - l * l) / c4;
+        sec = (l + r - (REAL)2 * c) / d2;
+        four = (ll - (REAL)4 * l + (REAL)6 * c - (REAL)4 * r + rr) / d4;
+    } else {
+        conv = (r * r - l * l) * c4;
+        sec = (l + r - (REAL)2 * c) * d2;
+        four = (ll - (REAL)4 * l + (REAL)6 * c - (REAL)4 * r + rr) * d4;
+    }
     return conv + sec + four;
 }
 /* stutterStep, KS1D_SweptShared.cu:159-164 */

@@ -146,3 +146,17 @@ def test_npy_rows_equal_dat_rows(sw, oracle, tmp_path, prob, prec):
         np.testing.assert_array_equal(rn[-4][2], fin.reshape(-1, 3)[1:-1, 0])
     else:
         np.testing.assert_array_equal(rn[-1][2], fin)
+
+
+def test_ks_divide_environment(sw, tmp_path):
+    """SWEPT1D_KS_DIVIDE=1 selects the DIVISE build's division form; at the
+    programs' dx = 0.5 it writes the same file as the reciprocal form."""
+    import os
+    files = []
+    for env in ("0", "1"):
+        out = tmp_path / ("ks_%s.dat" % env)
+        r = subprocess.run([str(_bin(sw, "KSDoubleOut")), "1024", "128", "0.005", "2", "0.5", "1", str(out)],
+                           capture_output=True, text=True, timeout=600, env=dict(os.environ, SWEPT1D_KS_DIVIDE=env))
+        assert r.returncode == 0, r.stdout + r.stderr
+        files.append(out.read_bytes())
+    assert files[0] == files[1]
