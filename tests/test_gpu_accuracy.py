@@ -101,3 +101,27 @@ def test_sod_convergence(sw, solver):
         errs.append(e)
         print("  nx = %6d: L1 %.3e" % (nx, e))
     assert errs[0] > errs[1] > errs[2] and errs[1] < 1e-3
+
+
+def test_ks_dt_sweep_against_reference_golden(sw, solver, golden):
+    """The reference's own accuracy procedure for KS (testProcedure.py:242-253:
+    nx = 1024, tpb = 64, dt from 1e-4 down) against its golden run
+    (Testing/KSDouble_Official.txt: FP64 swept, dt = 1e-7) at t = 6, with three
+    larger steps added where the scheme's O(dt^2) error is above the file's
+    10-digit resolution (~5e-10 at |u| < 10)."""
+    g = golden["ks"]
+    want = g["velocity"][1]
+    assert float(g["times"][1]) == 6.0
+    dts = (2e-3, 1e-3, 5e-4, 1e-4, 5e-5, 1e-5)
+    errs = []
+    print("\nKS FP64 swept, nx = 1024, tpb = 64, t = 6, against the reference's golden run (dt = 1e-7)")
+    for dt in dts:
+        cfg = sw.make_config(KS, 8, nx=1024)
+        ic = sw.initial_condition(cfg)
+        u = _advance(sw, solver, KS, 1024, 64, dt, ic, int(round(6.0 / dt)))
+        e = float(np.abs(u - want).max())
+        errs.append(e)
+        print("  dt = %-6g max |err| %.3e" % (dt, e))
+    for a, b in zip(errs[:2], errs[1:3]):
+        assert 3.0 < a / b < 5.0, errs  # second order in dt
+    assert max(errs[3:]) < 1.5e-9, errs  # at the golden file's resolution
