@@ -327,9 +327,21 @@ __device__ __forceinline__ void euler_level(const Params<T> &p, T *rows, int L, 
 // runs euler_level.
 enum TilePath { PATH_ANY = 0, PATH_CELL = 1, PATH_SPAN4 = 2 };
 
-// One sub-step of parity `par` on tile cells [lo, hi).  The one-cell-per-thread
-// loop starts at lo, so the live cells of a level start at the lowest thread:
-// whole warps idle, not part-empty ones.
+// Heat / KS cells [lo, hi) of one level, one per thread from the lowest thread,
+// so the live cells start at thread 0: whole warps idle, not part-empty ones.
+// A block with a thread for every tile cell needs one pass (hi - lo <= W).
+template <int P, typename T>
+__device__ __forceinline__ void tile_cells(const Params<T> &p, T *rows, int L, int W, int par, int lo, int hi,
+                                           Ends e) {
+    if ((int)blockDim.x >= W) {
+        const int x = lo + (int)threadIdx.x;
+        if (x < hi) tile_point<P, T>(p, rows, L, par, x, e);
+    } else {
+        for (int x = lo + (int)threadIdx.x; x < hi; x += blockDim.x) tile_point<P, T>(p, rows, L, par, x, e);
+    }
+}
+
+// One sub-step of parity `par` on tile cells [lo, hi).
 template <int P, typename T, int PATH>
 __device__ __forceinline__ void tile_level(const Params<T> &p, T *rows, int L, int W, int par, int lo, int hi,
                                            Ends e) {
@@ -338,24 +350,37 @@ __device__ __forceinline__ void tile_level(const Params<T> &p, T *rows, int L, i
     } else if constexpr (PATH == PATH_SPAN4) {
         tile_span4<P, T>(p, rows, L, par, lo, hi, e);
     } else if constexpr (PATH == PATH_CELL) {
-        for (int x = lo + (int)threadIdx.x; x < hi; x += blockDim.x) tile_point<P, T>(p, rows, L, par, x, e);
+        tile_cells<P, T>(p, rows, L, W, par, lo, hi, e);
     } else {
         if ((int)blockDim.x * 4 == W) {
             tile_span4<P, T>(p, rows, L, par, lo, hi, e);
         } else {
-            for (int x = lo + (int)threadIdx.x; x < hi; x += blockDim.x) tile_point<P, T>(p, rows, L, par, x, e);
+            tile_cells<P, T>(p, rows, L, W, par, lo, hi, e);
         }
     }
 }
 
+// Heat and KS take the level loops two levels at a time, so each level's
+// parity (which row it reads and which it writes) is a constant; H = W / 2R is
+// even, W being a multiple of 32.  Euler's long levels gain nothing from it and
+// its persistent kernels would spill, so it keeps one level per iteration.
 // Down part: sub-steps j = 1..H on the growing centre [W/2 - jR, W/2 + jR).
 template <int P, typename T, int PATH = PATH_ANY>
 __device__ __forceinline__ void tile_down(const Params<T> &p, T *rows, int L, int W, int64_t base) {
     constexpr int R = Scheme<P, T>::R;
     const int h = W >> 1, H = W / (2 * R);
     const Ends e = tile_ends(base, p.nx, W, R);
-    for (int j = 1; j <= H; ++j) {
-        tile_level<P, T, PATH>(p, rows, L, W, j & 1, h - j * R, h + j * R, e);
+    if constexpr (P == SW_EULER) {
+        for (int j = 1; j <= H; ++j) {
+            tile_level<P, T, PATH>(p, rows, L, W, j & 1, h - j * R, h + j * R, e);
+            __syncthreads();
+        }
+        return;
+    }
+    for (int j = 1; j < H; j += 2) {
+        tile_level<P, T, PATH>(p, rows, L, W, 1, h - j * R, h + j * R, e);
+        __syncthreads();
+        tile_level<P, T, PATH>(p, rows, L, W, 0, h - (j + 1) * R, h + (j + 1) * R, e);
         __syncthreads();
     }
 }
@@ -365,10 +390,22 @@ __device__ __forceinline__ void tile_up(const Params<T> &p, T *rows, int L, int 
     constexpr int R = Scheme<P, T>::R;
     const int H = W / (2 * R);
     const Ends e = tile_ends(base, p.nx, W, R);
-    for (int u = 1; u < H; ++u) {
-        tile_level<P, T, PATH>(p, rows, L, W, u & 1, u * R, W - u * R, e);
+    if constexpr (P == SW_EULER) {
+        for (int u = 1; u < H; ++u) {
+            tile_level<P, T, PATH>(p, rows, L, W, u & 1, u * R, W - u * R, e);
+            __syncthreads();
+        }
+        return;
+    }
+    int u = 1;
+    for (; u + 1 < H; u += 2) {
+        tile_level<P, T, PATH>(p, rows, L, W, 1, u * R, W - u * R, e);
+        __syncthreads();
+        tile_level<P, T, PATH>(p, rows, L, W, 0, (u + 1) * R, W - (u + 1) * R, e);
         __syncthreads();
     }
+    tile_level<P, T, PATH>(p, rows, L, W, 1, u * R, W - u * R, e);  // u = H - 1, odd
+    __syncthreads();
 }
 
 // Default threads per swept block.  FP32 Heat / KS run 4 contiguous cells per
