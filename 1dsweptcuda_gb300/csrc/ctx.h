@@ -78,6 +78,7 @@ inline Params<T> make_params(const sw_config &c, const sw_constants &k) {
     for (int i = 0; i < 6; ++i) p.bd[i] = (T)k.bd[i];
     p.nx = c.nx;
     p.bc = resolved_bc(c);
+    p.nz = -T(0);
     auto is_pow2 = [](T v) {
         int e = 0;
         return v > T(0) && std::isfinite((double)v) && std::frexp((double)v, &e) == 0.5;

@@ -103,6 +103,23 @@ __device__ __forceinline__ T ks_correct_sq(const Params<T> &p, T u, T ll, T l, T
     return ad(u, ml(-p.dt, ks_rhs_sq(p, ll, l, c, r, rr, l2, r2)));
 }
 
+// ------------------------------------------------- paired FP32 (sm_100+)
+// Two cells per instruction with the f32x2 add and fma (__fadd2_rn,
+// __ffma2_rn).  Each component rounds as its scalar counterpart does, so a
+// pair gives the same bits as two scalar evaluations -- provided no multiply
+// is merged with a following add into one fma, which the compiler was found to
+// do with the f32x2 multiply even with -fmad=false.  So a product is always
+// formed as fma(a, b, nz) with nz = -0.0 passed at run time (Params::nz): the
+// same single rounding of a * b, and an fma is never merged again.
+__device__ __forceinline__ float2 dup2(float v) { return make_float2(v, v); }
+__device__ __forceinline__ float2 ad2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 ml2(const Params<float> &p, float2 a, float2 b) { return __ffma2_rn(a, b, dup2(p.nz)); }
+
+// heat_step on a pair of cells
+__device__ __forceinline__ float2 heat_step2(const Params<float> &p, float2 l, float2 c, float2 r) {
+    return ad2(ml2(p, dup2(p.fo), ad2(l, r)), ml2(p, dup2(p.fo2), c));
+}
+
 // --------------------------------------------------------------- Euler
 template <typename T>
 struct Q3 {

@@ -21,6 +21,7 @@ struct Params {
     int64_t nx;
     int bc;                    // SW_BC_MIRROR / PERIODIC / DIRICHLET
     int ks_form;               // KS: how c4, d2, d4 enter the right-hand side (enum KsForm)
+    T nz;                      // -0.0, the addend that makes an fma a plain product (paired FP32 path)
 };
 
 // KS right-hand-side forms.  KS_POW2: c4, d2, d4 are exact powers of two, so
