@@ -165,37 +165,44 @@ __device__ __forceinline__ void tile_fix_bc(const Params<T> &p, T *rows, int L, 
 }
 
 // Slot layout of half-tile h: cells [h*W, h*W + W/2) = row 0, [h*W + W/2, (h+1)*W) = row 1.
+// Element i (0 <= i < W) of a tile's import / export: two values, one per row.
+template <int P, typename T>
+__device__ __forceinline__ void tile_import_at(T *rows, int L, int W, const typename Scheme<P, T>::G *sl,
+                                               const typename Scheme<P, T>::G *sr, int i) {
+    constexpr int R = Scheme<P, T>::R;
+    const int h = W >> 1;
+    if (i < h) {
+        tile_put<P, T>(rows, L, 0, i, sl[i]);
+        tile_put<P, T>(rows, L, 1, i - R, sl[h + i]);
+    } else {
+        const int j = i - h;
+        tile_put<P, T>(rows, L, 0, h + j, sr[j]);
+        tile_put<P, T>(rows, L, 1, h + R + j, sr[h + j]);
+    }
+}
+template <int P, typename T>
+__device__ __forceinline__ void tile_export_at(const T *rows, int L, int W, typename Scheme<P, T>::G *sl,
+                                               typename Scheme<P, T>::G *sr, int i) {
+    constexpr int R = Scheme<P, T>::R;
+    const int h = W >> 1;
+    if (i < h) {
+        sl[i] = tile_get<P, T>(rows, L, 0, i);
+        sl[h + i] = tile_get<P, T>(rows, L, 1, R + i);
+    } else {
+        const int j = i - h;
+        sr[j] = tile_get<P, T>(rows, L, 0, h + j);
+        sr[h + j] = tile_get<P, T>(rows, L, 1, h - R + j);
+    }
+}
 template <int P, typename T>
 __device__ __forceinline__ void tile_import(T *rows, int L, int W, const typename Scheme<P, T>::G *sl,
                                             const typename Scheme<P, T>::G *sr) {
-    constexpr int R = Scheme<P, T>::R;
-    const int h = W >> 1;
-    for (int i = threadIdx.x; i < W; i += blockDim.x) {
-        if (i < h) {
-            tile_put<P, T>(rows, L, 0, i, sl[i]);
-            tile_put<P, T>(rows, L, 1, i - R, sl[h + i]);
-        } else {
-            const int j = i - h;
-            tile_put<P, T>(rows, L, 0, h + j, sr[j]);
-            tile_put<P, T>(rows, L, 1, h + R + j, sr[h + j]);
-        }
-    }
+    for (int i = threadIdx.x; i < W; i += blockDim.x) tile_import_at<P, T>(rows, L, W, sl, sr, i);
 }
 template <int P, typename T>
 __device__ __forceinline__ void tile_export(const T *rows, int L, int W, typename Scheme<P, T>::G *sl,
                                             typename Scheme<P, T>::G *sr) {
-    constexpr int R = Scheme<P, T>::R;
-    const int h = W >> 1;
-    for (int i = threadIdx.x; i < W; i += blockDim.x) {
-        if (i < h) {
-            sl[i] = tile_get<P, T>(rows, L, 0, i);
-            sl[h + i] = tile_get<P, T>(rows, L, 1, R + i);
-        } else {
-            const int j = i - h;
-            sr[j] = tile_get<P, T>(rows, L, 0, h + j);
-            sr[h + j] = tile_get<P, T>(rows, L, 1, h - R + j);
-        }
-    }
+    for (int i = threadIdx.x; i < W; i += blockDim.x) tile_export_at<P, T>(rows, L, W, sl, sr, i);
 }
 
 // Aligned 4-value shared-memory loads.
@@ -602,6 +609,91 @@ __global__ void k_unpack3(const V4<T> *__restrict__ in4, T *__restrict__ out3, i
     }
 }
 
+// ------------------------------------------------ G tiles per block (Heat, KS)
+// An FP64 warp instruction holds its SM sub-partition's FP64 pipe for the same
+// time whatever number of its lanes are active (a probe measured 64 cycles per
+// DADD for 1 to 32 lanes), so the part-empty top warp of every level costs a
+// full warp of FP64 time.  A block of G*W threads holds tiles t0 .. t0 + G - 1
+// (one cell per thread) and packs the G tiles' live cells of a level, the same
+// count n for each, onto threads 0 .. G*n - 1: one part-empty warp per level
+// instead of G.  Same cells, same arithmetic (tile_point) as swept_tile.
+template <int G>
+__device__ __forceinline__ int group_slot(int t, int n) {
+    int k = 0;
+#pragma unroll
+    for (int q = 1; q < G; ++q) k += (t >= q * n) ? 1 : 0;
+    return k;
+}
+template <int P, typename T, int G>
+__device__ __forceinline__ void group_level(const Params<T> &p, T *rows, int TS, int L, int par, int lo, int hi,
+                                            const Ends (&e)[G]) {
+    const int n = hi - lo, t = (int)threadIdx.x;
+    if (t < G * n) {
+        const int k = group_slot<G>(t, n);
+        Ends ek = e[0];
+#pragma unroll
+        for (int q = 1; q < G; ++q)
+            if (k == q) ek = e[q];
+        tile_point<P, T>(p, rows + k * TS, L, par, lo + t - k * n, ek);
+    }
+}
+
+template <int P, typename T, int MODE, int G>
+__device__ __forceinline__ void swept_tile_group(const Params<T> &p, T *__restrict__ state, T *__restrict__ slots,
+                                                 T *rows, const int W, const int phase, const int64_t t0) {
+    static_assert(P != SW_EULER, "Euler levels run euler_level");
+    constexpr int R = Scheme<P, T>::R;
+    const int L = row_stride(W), h = W >> 1, H = W / (2 * R), TS = tile_rows<P>() * L;
+    const int64_t nx = p.nx, nhalf = nx / h;
+    int64_t base[G], hl[G], hr[G];
+    Ends e[G];
+#pragma unroll
+    for (int k = 0; k < G; ++k) {
+        base[k] = (t0 + k) * W + (int64_t)phase * h;
+        hl[k] = (2 * (t0 + k) + phase) % nhalf;
+        hr[k] = (hl[k] + 1 == nhalf) ? 0 : hl[k] + 1;
+        e[k] = tile_ends(base[k], nx, W, R);
+    }
+    // import / export: thread i handles element i % W of tile i / W (blockDim.x == G * W)
+    const int ki = (int)threadIdx.x / W, xi = (int)threadIdx.x - ki * W;
+    if constexpr (MODE == MODE_UP) tile_put<P, T>(rows + ki * TS, L, 0, xi, state[base[ki] + xi]);
+    else tile_import_at<P, T>(rows + ki * TS, L, W, slots + hl[ki] * W, slots + hr[ki] * W, xi);
+    __syncthreads();
+    if constexpr (MODE != MODE_UP) {  // down part, two levels per iteration (H is even)
+        for (int j = 1; j < H; j += 2) {
+            group_level<P, T, G>(p, rows, TS, L, 1, h - j * R, h + j * R, e);
+            __syncthreads();
+            group_level<P, T, G>(p, rows, TS, L, 0, h - (j + 1) * R, h + (j + 1) * R, e);
+            __syncthreads();
+        }
+    }
+    if constexpr (MODE == MODE_DOWN) {
+        state[wrap_pos(base[ki] + xi, nx)] = tile_get<P, T>(rows + ki * TS, L, 0, xi);
+    } else {
+        int u = 1;
+        for (; u + 1 < H; u += 2) {
+            group_level<P, T, G>(p, rows, TS, L, 1, u * R, W - u * R, e);
+            __syncthreads();
+            group_level<P, T, G>(p, rows, TS, L, 0, (u + 1) * R, W - (u + 1) * R, e);
+            __syncthreads();
+        }
+        group_level<P, T, G>(p, rows, TS, L, 1, u * R, W - u * R, e);  // u = H - 1
+        __syncthreads();
+        tile_export_at<P, T>(rows + ki * TS, L, W, slots + hl[ki] * W, slots + hr[ki] * W, xi);
+    }
+}
+
+template <int P, typename T, int MODE, int G>
+__global__ void __launch_bounds__(1024) k_swept_group(const Params<T> p, T *__restrict__ state,
+                                                      T *__restrict__ slots, const int W, const int phase) {
+    extern __shared__ __align__(16) unsigned char sw_smem[];
+    swept_tile_group<P, T, MODE, G>(p, state, slots, reinterpret_cast<T *>(sw_smem), W, phase,
+                                    G * (int64_t)blockIdx.x);
+}
+
+// Grouped tiles pay where blocks are plentiful: a domain of at least this many tiles.
+constexpr int64_t kGroupMinTiles = 1024;
+
 // ------------------------------------------------------------- launchers
 // The dynamic shared-memory limit above the 48 KB default, set once per
 // (launcher, device): the attribute belongs to the device that is current when
@@ -761,6 +853,24 @@ __global__ void __launch_bounds__(32 * kKsWarpTilesPerBlock)
     }
 }
 
+template <int P, typename T, int G>
+cudaError_t launch_swept_group(const Params<T> &p, int mode, int phase, T *st, T *sl, int64_t nx, int W,
+                               cudaStream_t s) {
+    static SmemOnce once;
+    cudaError_t e = once.ensure(k_swept_group<P, T, MODE_UP, G>, k_swept_group<P, T, MODE_DIAMOND, G>,
+                                k_swept_group<P, T, MODE_DOWN, G>);
+    if (e != cudaSuccess) return e;
+    const size_t smem = G * swept_smem_bytes<P, T>(W);
+    const unsigned grid = (unsigned)(nx / W / G);
+    const int threads = G * W;
+    switch (mode) {
+    case MODE_UP: k_swept_group<P, T, MODE_UP, G><<<grid, threads, smem, s>>>(p, st, sl, W, phase); break;
+    case MODE_DIAMOND: k_swept_group<P, T, MODE_DIAMOND, G><<<grid, threads, smem, s>>>(p, st, sl, W, phase); break;
+    default: k_swept_group<P, T, MODE_DOWN, G><<<grid, threads, smem, s>>>(p, st, sl, W, phase); break;
+    }
+    return cudaGetLastError();
+}
+
 template <typename T>
 cudaError_t launch_swept_ks_warp(const Params<T> &p, int mode, int phase, T *st, T *sl, int64_t nx, cudaStream_t s) {
     const int64_t ntile = nx / kKsWarpTile;
@@ -786,6 +896,17 @@ cudaError_t launch_swept(const void *vp, int mode, int phase, void *state, void 
     }
     if constexpr (P != SW_EULER) {
         if (threads * 4 == W) return launch_swept_path<P, T, PATH_SPAN4>(p, mode, phase, st, sl, nx, W, threads, s);
+        // The default one-cell-per-thread shape on a large domain: G tiles per block.  KS
+        // takes up to four tiles and 1024 threads; Heat, whose levels are four FP64
+        // operations, two tiles and 512 threads (four measured 3 % slower than two).
+        const int64_t ntiles = nx / W;
+        constexpr int kMaxThreads = (P == SW_KS) ? 1024 : 512;
+        if (threads_req == 0 && threads == W && ntiles >= kGroupMinTiles) {
+            if (P == SW_KS && 4 * W <= kMaxThreads && ntiles % 4 == 0)
+                return launch_swept_group<P, T, 4>(p, mode, phase, st, sl, nx, W, s);
+            if (2 * W <= kMaxThreads && ntiles % 2 == 0)
+                return launch_swept_group<P, T, 2>(p, mode, phase, st, sl, nx, W, s);
+        }
     }
     return launch_swept_path<P, T, PATH_CELL>(p, mode, phase, st, sl, nx, W, threads, s);
 }

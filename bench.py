@@ -284,7 +284,8 @@ def run_ours(args) -> None:
     steps_per_launch = TPB // 8
     alg_bytes = B_CLASSIC_KS_F64 * NX * steps_per_launch
     achieved = alg_bytes / (launch_ms * 1e-3) / 1e9
-    roof = {"bound": "hbm", "kernel": "k_swept<KS,double,DIAMOND>", "achieved": achieved, "peak": hbm,
+    roof = {"bound": "hbm", "kernel": "k_swept_group<KS,double,DIAMOND,4> (four 256-cell tiles per block)",
+            "achieved": achieved, "peak": hbm,
             "unit": "GB/s", "frac": achieved / hbm, "peak_source": peak_src,
             "traffic": DIAMOND_TRAFFIC_BYTES, "traffic_source": "ncu dram__bytes_read+write, one diamond launch",
             "launch_ms": launch_ms,

@@ -115,6 +115,23 @@ def test_threads_per_block(sw, solver, oracle, problem, prec):
             _assert_identical(got, want, "problem %d prec %d alg %d threads %d" % (problem, prec, alg, th))
 
 
+@pytest.mark.parametrize("problem, prec, tpb, bc", [(KS, 8, 64, 0), (KS, 4, 64, 0), (HEAT, 8, 32, 0),
+                                                    (HEAT, 8, 64, 2), (HEAT, 4, 32, 0), (KS, 8, 512, 0)])
+def test_grouped_tiles(sw, solver, oracle, problem, prec, tpb, bc):
+    """Domains of >= 1024 tiles with the default one-cell-per-thread shape run
+    several tiles per block (KS four, two at tpb 512; Heat two), their live
+    cells packed together at every level."""
+    nx = 1024 * tpb
+    dt = PROBLEM_DT[problem]
+    c = _case(oracle, problem, prec, nx, dt, bc=oracle.BC_PERIODIC if bc == 2 else None)
+    ic = _ic(oracle, problem, prec, nx, kind="random", seed=21)
+    q = tpb // (2 * oracle.RADIUS[problem] * oracle.SUBSTEPS[problem])
+    for nsteps in (q, 3 * q + 1):
+        want = oracle.classic(c, ic, nsteps)
+        got, _ = _gpu(sw, solver, problem, prec, SWEPT, nx, tpb, dt, nsteps, ic, bc=bc)
+        _assert_identical(got, want, "problem %d prec %d tpb %d bc %d steps %d" % (problem, prec, tpb, bc, nsteps))
+
+
 @pytest.mark.parametrize("prec", [8, 4])
 def test_heat_periodic(sw, solver, oracle, prec):
     """Heat on a periodic domain (the benchmark's boundary), all paths."""
