@@ -54,8 +54,8 @@ WORKLOAD = ("KS1D FP64 swept (alg 1), periodic, nx=2^20, tpb=256, dx=0.5, dt=0.0
             "(40000 time steps per step)")
 K40_KS_F64_SWEPT_PUBLISHED = 1.07e10  # the reference's published KS FP64 swept figure, nx=2^20, on a K40c
 # DRAM bytes (read + write) of one diamond launch of this workload from one ncu
-# capture of this launch (cold-cache replay).
-DIAMOND_TRAFFIC_BYTES = 16800000
+# capture of this launch (cold-cache replay): 16.80 MB read + 0.84 MB written.
+DIAMOND_TRAFFIC_BYTES = 17640000
 
 
 def _peaks():
