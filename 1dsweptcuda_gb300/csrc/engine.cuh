@@ -238,10 +238,12 @@ __device__ __forceinline__ void store_pairs(double *p, const double *w) {
 // window of source cells x0 - R .. x0 + 7 - R with two aligned vector loads and
 // updates those of its cells x0 .. x0 + 3 that lie in [lo, hi).  Same
 // arithmetic as tile_point, cell for cell.
+// (tid: the thread's index among the tile's threads)
 template <int P, typename T>
-__device__ __forceinline__ void tile_span4(const Params<T> &p, T *rows, int L, int par, int lo, int hi, Ends e) {
+__device__ __forceinline__ void tile_span4(const Params<T> &p, T *rows, int L, int par, int lo, int hi, Ends e,
+                                           const int tid) {
     constexpr int R = Scheme<P, T>::R;
-    const int x0 = (lo & ~3) + (int)threadIdx.x * 4;
+    const int x0 = (lo & ~3) + tid * 4;
     if (x0 >= hi) return;
     const T *src = rows + (par ^ 1) * L;
     T *dst = rows + par * L + R;
@@ -369,12 +371,12 @@ __device__ __forceinline__ void tile_level(const Params<T> &p, T *rows, int L, i
     if constexpr (P == SW_EULER) {
         euler_level<T>(p, rows, L, W, par, lo, hi, e);
     } else if constexpr (PATH == PATH_SPAN4) {
-        tile_span4<P, T>(p, rows, L, par, lo, hi, e);
+        tile_span4<P, T>(p, rows, L, par, lo, hi, e, (int)threadIdx.x);
     } else if constexpr (PATH == PATH_CELL) {
         tile_cells<P, T>(p, rows, L, W, par, lo, hi, e);
     } else {
         if ((int)blockDim.x * 4 == W) {
-            tile_span4<P, T>(p, rows, L, par, lo, hi, e);
+            tile_span4<P, T>(p, rows, L, par, lo, hi, e, (int)threadIdx.x);
         } else {
             tile_cells<P, T>(p, rows, L, W, par, lo, hi, e);
         }
@@ -613,10 +615,11 @@ __global__ void k_unpack3(const V4<T> *__restrict__ in4, T *__restrict__ out3, i
 // An FP64 warp instruction holds its SM sub-partition's FP64 pipe for the same
 // time whatever number of its lanes are active (a probe measured 64 cycles per
 // DADD for 1 to 32 lanes), so the part-empty top warp of every level costs a
-// full warp of FP64 time.  A block of G*W threads holds tiles t0 .. t0 + G - 1
-// (one cell per thread) and packs the G tiles' live cells of a level, the same
-// count n for each, onto threads 0 .. G*n - 1: one part-empty warp per level
-// instead of G.  Same cells, same arithmetic (tile_point) as swept_tile.
+// full warp of FP64 time (and an issue slot in FP32).  A block holds tiles
+// t0 .. t0 + G - 1 and packs the G tiles' live cells of a level, the same
+// count for each, onto its lowest threads: one part-empty warp per level
+// instead of G.  PATH_CELL: one cell per thread (G*W threads); PATH_SPAN4: four
+// cells per thread (G*W/4 threads).  Same cells, same arithmetic as swept_tile.
 template <int G>
 __device__ __forceinline__ int group_slot(int t, int n) {
     int k = 0;
@@ -624,21 +627,24 @@ __device__ __forceinline__ int group_slot(int t, int n) {
     for (int q = 1; q < G; ++q) k += (t >= q * n) ? 1 : 0;
     return k;
 }
-template <int P, typename T, int G>
+template <int P, typename T, int G, int PATH>
 __device__ __forceinline__ void group_level(const Params<T> &p, T *rows, int TS, int L, int par, int lo, int hi,
                                             const Ends (&e)[G]) {
-    const int n = hi - lo, t = (int)threadIdx.x;
+    // threads per tile at this level
+    const int n = (PATH == PATH_SPAN4) ? ((hi - (lo & ~3) + 3) >> 2) : (hi - lo);
+    const int t = (int)threadIdx.x;
     if (t < G * n) {
         const int k = group_slot<G>(t, n);
         Ends ek = e[0];
 #pragma unroll
         for (int q = 1; q < G; ++q)
             if (k == q) ek = e[q];
-        tile_point<P, T>(p, rows + k * TS, L, par, lo + t - k * n, ek);
+        if constexpr (PATH == PATH_SPAN4) tile_span4<P, T>(p, rows + k * TS, L, par, lo, hi, ek, t - k * n);
+        else tile_point<P, T>(p, rows + k * TS, L, par, lo + t - k * n, ek);
     }
 }
 
-template <int P, typename T, int MODE, int G>
+template <int P, typename T, int MODE, int G, int PATH>
 __device__ __forceinline__ void swept_tile_group(const Params<T> &p, T *__restrict__ state, T *__restrict__ slots,
                                                  T *rows, const int W, const int phase, const int64_t t0) {
     static_assert(P != SW_EULER, "Euler levels run euler_level");
@@ -654,41 +660,49 @@ __device__ __forceinline__ void swept_tile_group(const Params<T> &p, T *__restri
         hr[k] = (hl[k] + 1 == nhalf) ? 0 : hl[k] + 1;
         e[k] = tile_ends(base[k], nx, W, R);
     }
-    // import / export: thread i handles element i % W of tile i / W (blockDim.x == G * W)
-    const int ki = (int)threadIdx.x / W, xi = (int)threadIdx.x - ki * W;
-    if constexpr (MODE == MODE_UP) tile_put<P, T>(rows + ki * TS, L, 0, xi, state[base[ki] + xi]);
-    else tile_import_at<P, T>(rows + ki * TS, L, W, slots + hl[ki] * W, slots + hr[ki] * W, xi);
+    // import / export: element i of the block is element i % W of tile i / W
+    for (int i = threadIdx.x; i < G * W; i += blockDim.x) {
+        const int k = i / W, x = i - k * W;
+        if constexpr (MODE == MODE_UP) tile_put<P, T>(rows + k * TS, L, 0, x, state[base[k] + x]);
+        else tile_import_at<P, T>(rows + k * TS, L, W, slots + hl[k] * W, slots + hr[k] * W, x);
+    }
     __syncthreads();
     if constexpr (MODE != MODE_UP) {  // down part, two levels per iteration (H is even)
         for (int j = 1; j < H; j += 2) {
-            group_level<P, T, G>(p, rows, TS, L, 1, h - j * R, h + j * R, e);
+            group_level<P, T, G, PATH>(p, rows, TS, L, 1, h - j * R, h + j * R, e);
             __syncthreads();
-            group_level<P, T, G>(p, rows, TS, L, 0, h - (j + 1) * R, h + (j + 1) * R, e);
+            group_level<P, T, G, PATH>(p, rows, TS, L, 0, h - (j + 1) * R, h + (j + 1) * R, e);
             __syncthreads();
         }
     }
     if constexpr (MODE == MODE_DOWN) {
-        state[wrap_pos(base[ki] + xi, nx)] = tile_get<P, T>(rows + ki * TS, L, 0, xi);
+        for (int i = threadIdx.x; i < G * W; i += blockDim.x) {
+            const int k = i / W, x = i - k * W;
+            state[wrap_pos(base[k] + x, nx)] = tile_get<P, T>(rows + k * TS, L, 0, x);
+        }
     } else {
         int u = 1;
         for (; u + 1 < H; u += 2) {
-            group_level<P, T, G>(p, rows, TS, L, 1, u * R, W - u * R, e);
+            group_level<P, T, G, PATH>(p, rows, TS, L, 1, u * R, W - u * R, e);
             __syncthreads();
-            group_level<P, T, G>(p, rows, TS, L, 0, (u + 1) * R, W - (u + 1) * R, e);
+            group_level<P, T, G, PATH>(p, rows, TS, L, 0, (u + 1) * R, W - (u + 1) * R, e);
             __syncthreads();
         }
-        group_level<P, T, G>(p, rows, TS, L, 1, u * R, W - u * R, e);  // u = H - 1
+        group_level<P, T, G, PATH>(p, rows, TS, L, 1, u * R, W - u * R, e);  // u = H - 1
         __syncthreads();
-        tile_export_at<P, T>(rows + ki * TS, L, W, slots + hl[ki] * W, slots + hr[ki] * W, xi);
+        for (int i = threadIdx.x; i < G * W; i += blockDim.x) {
+            const int k = i / W, x = i - k * W;
+            tile_export_at<P, T>(rows + k * TS, L, W, slots + hl[k] * W, slots + hr[k] * W, x);
+        }
     }
 }
 
-template <int P, typename T, int MODE, int G>
+template <int P, typename T, int MODE, int G, int PATH>
 __global__ void __launch_bounds__(1024) k_swept_group(const Params<T> p, T *__restrict__ state,
                                                       T *__restrict__ slots, const int W, const int phase) {
     extern __shared__ __align__(16) unsigned char sw_smem[];
-    swept_tile_group<P, T, MODE, G>(p, state, slots, reinterpret_cast<T *>(sw_smem), W, phase,
-                                    G * (int64_t)blockIdx.x);
+    swept_tile_group<P, T, MODE, G, PATH>(p, state, slots, reinterpret_cast<T *>(sw_smem), W, phase,
+                                          G * (int64_t)blockIdx.x);
 }
 
 // Grouped tiles pay where blocks are plentiful: a domain of at least this many tiles.
@@ -853,20 +867,22 @@ __global__ void __launch_bounds__(32 * kKsWarpTilesPerBlock)
     }
 }
 
-template <int P, typename T, int G>
+template <int P, typename T, int G, int PATH>
 cudaError_t launch_swept_group(const Params<T> &p, int mode, int phase, T *st, T *sl, int64_t nx, int W,
-                               cudaStream_t s) {
+                               int threads, cudaStream_t s) {
     static SmemOnce once;
-    cudaError_t e = once.ensure(k_swept_group<P, T, MODE_UP, G>, k_swept_group<P, T, MODE_DIAMOND, G>,
-                                k_swept_group<P, T, MODE_DOWN, G>);
+    cudaError_t e = once.ensure(k_swept_group<P, T, MODE_UP, G, PATH>, k_swept_group<P, T, MODE_DIAMOND, G, PATH>,
+                                k_swept_group<P, T, MODE_DOWN, G, PATH>);
     if (e != cudaSuccess) return e;
     const size_t smem = G * swept_smem_bytes<P, T>(W);
     const unsigned grid = (unsigned)(nx / W / G);
-    const int threads = G * W;
+    const int block = G * threads;
     switch (mode) {
-    case MODE_UP: k_swept_group<P, T, MODE_UP, G><<<grid, threads, smem, s>>>(p, st, sl, W, phase); break;
-    case MODE_DIAMOND: k_swept_group<P, T, MODE_DIAMOND, G><<<grid, threads, smem, s>>>(p, st, sl, W, phase); break;
-    default: k_swept_group<P, T, MODE_DOWN, G><<<grid, threads, smem, s>>>(p, st, sl, W, phase); break;
+    case MODE_UP: k_swept_group<P, T, MODE_UP, G, PATH><<<grid, block, smem, s>>>(p, st, sl, W, phase); break;
+    case MODE_DIAMOND:
+        k_swept_group<P, T, MODE_DIAMOND, G, PATH><<<grid, block, smem, s>>>(p, st, sl, W, phase);
+        break;
+    default: k_swept_group<P, T, MODE_DOWN, G, PATH><<<grid, block, smem, s>>>(p, st, sl, W, phase); break;
     }
     return cudaGetLastError();
 }
@@ -895,17 +911,26 @@ cudaError_t launch_swept(const void *vp, int mode, int phase, void *state, void 
         if (W == kKsWarpTile && threads == 32) return launch_swept_ks_warp<T>(p, mode, phase, st, sl, nx, s);
     }
     if constexpr (P != SW_EULER) {
-        if (threads * 4 == W) return launch_swept_path<P, T, PATH_SPAN4>(p, mode, phase, st, sl, nx, W, threads, s);
-        // The default one-cell-per-thread shape on a large domain: G tiles per block.  KS
-        // takes up to four tiles and 1024 threads; Heat, whose levels are four FP64
+        // The default shapes on a large domain: G tiles per block.  One cell per thread:
+        // KS up to four tiles and 1024 threads; Heat, whose levels are four FP64
         // operations, two tiles and 512 threads (four measured 3 % slower than two).
+        // Four cells per thread: tiles up to 256 cells only (KS four, Heat two; +6 % at
+        // 256 cells), since at 1024 cells grouping measured 7 % (Heat) and 25 % (KS) slower.
         const int64_t ntiles = nx / W;
+        const bool group = threads_req == 0 && ntiles >= kGroupMinTiles;
+        if (threads * 4 == W) {
+            if (group && W <= 256 && P == SW_KS && ntiles % 4 == 0)
+                return launch_swept_group<P, T, 4, PATH_SPAN4>(p, mode, phase, st, sl, nx, W, threads, s);
+            if (group && W <= 256 && ntiles % 2 == 0)
+                return launch_swept_group<P, T, 2, PATH_SPAN4>(p, mode, phase, st, sl, nx, W, threads, s);
+            return launch_swept_path<P, T, PATH_SPAN4>(p, mode, phase, st, sl, nx, W, threads, s);
+        }
         constexpr int kMaxThreads = (P == SW_KS) ? 1024 : 512;
-        if (threads_req == 0 && threads == W && ntiles >= kGroupMinTiles) {
+        if (group && threads == W) {
             if (P == SW_KS && 4 * W <= kMaxThreads && ntiles % 4 == 0)
-                return launch_swept_group<P, T, 4>(p, mode, phase, st, sl, nx, W, s);
+                return launch_swept_group<P, T, 4, PATH_CELL>(p, mode, phase, st, sl, nx, W, threads, s);
             if (2 * W <= kMaxThreads && ntiles % 2 == 0)
-                return launch_swept_group<P, T, 2>(p, mode, phase, st, sl, nx, W, s);
+                return launch_swept_group<P, T, 2, PATH_CELL>(p, mode, phase, st, sl, nx, W, threads, s);
         }
     }
     return launch_swept_path<P, T, PATH_CELL>(p, mode, phase, st, sl, nx, W, threads, s);

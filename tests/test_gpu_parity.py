@@ -116,11 +116,13 @@ def test_threads_per_block(sw, solver, oracle, problem, prec):
 
 
 @pytest.mark.parametrize("problem, prec, tpb, bc", [(KS, 8, 64, 0), (KS, 4, 64, 0), (HEAT, 8, 32, 0),
-                                                    (HEAT, 8, 64, 2), (HEAT, 4, 32, 0), (KS, 8, 512, 0)])
+                                                    (HEAT, 8, 64, 2), (HEAT, 4, 32, 0), (KS, 8, 512, 0),
+                                                    (KS, 4, 256, 0), (HEAT, 4, 128, 0), (HEAT, 4, 128, 2)])
 def test_grouped_tiles(sw, solver, oracle, problem, prec, tpb, bc):
-    """Domains of >= 1024 tiles with the default one-cell-per-thread shape run
-    several tiles per block (KS four, two at tpb 512; Heat two), their live
-    cells packed together at every level."""
+    """Domains of >= 1024 tiles with the default thread shape run several tiles
+    per block (KS four, two at tpb 512; Heat two), their live cells packed
+    together at every level: one cell per thread, and 4 cells per thread in
+    FP32 from tpb 128 (KS from 256; its 128-cell tiles take the warp kernel)."""
     nx = 1024 * tpb
     dt = PROBLEM_DT[problem]
     c = _case(oracle, problem, prec, nx, dt, bc=oracle.BC_PERIODIC if bc == 2 else None)
