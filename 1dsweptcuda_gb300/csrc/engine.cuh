@@ -483,8 +483,14 @@ __device__ __forceinline__ void swept_tile(const Params<T> &p, typename Scheme<P
 }
 
 // One swept pass over all tiles of one domain; block = one tile.
+// FP32 four-cells-per-thread blocks ask for 2048 resident threads per SM (32 registers).
+template <int P, typename T, int PATH>
+constexpr int swept_min_blocks() {
+    return (PATH == PATH_SPAN4 && sizeof(T) == 4) ? 2048 / Scheme<P, T>::MAXT : 1;
+}
 template <int P, typename T, int MODE, int PATH>
-__global__ void __launch_bounds__(Scheme<P, T>::MAXT) k_swept(const Params<T> p, typename Scheme<P, T>::G *__restrict__ state,
+__global__ void __launch_bounds__(Scheme<P, T>::MAXT, (swept_min_blocks<P, T, PATH>()))
+    k_swept(const Params<T> p, typename Scheme<P, T>::G *__restrict__ state,
                                                 typename Scheme<P, T>::G *__restrict__ slots, const int W,
                                                 const int phase) {
     extern __shared__ __align__(16) unsigned char sw_smem[];

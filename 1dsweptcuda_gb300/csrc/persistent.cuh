@@ -286,7 +286,7 @@ cudaError_t launch_persistent_ks_smem_nodes(const Params<T> &p, T *st, T *sl, un
 // sw_internal.h, maps a global tile to its domain).
 
 template <int P, typename T, int MODE, int PATH>
-__global__ void __launch_bounds__(Scheme<P, T>::MAXT)
+__global__ void __launch_bounds__(Scheme<P, T>::MAXT, (swept_min_blocks<P, T, PATH>()))
     k_swept_batch(const Params<T> p, typename Scheme<P, T>::G *__restrict__ state,
                   typename Scheme<P, T>::G *__restrict__ slots, const BatchDev b, const int W, const int phase) {
     extern __shared__ __align__(16) unsigned char sw_smem[];
