@@ -100,7 +100,8 @@ typedef struct sw_config {
     double gamma;        /* Euler heat-capacity ratio 1.4 */
     double left[3];      /* Euler left state (rho, u, p); all 0 = Sod (1, 0, 1) */
     double right[3];     /* Euler right state (rho, u, p); all 0 = Sod (0.125, 0, 0.1) */
-    int32_t threads;     /* threads per swept block: 0 = the library's default for the tile width; a
+    int32_t threads;     /* threads per swept tile: 0 = the library's default for the tile width (on
+                            a domain of >= 1024 tiles one block may then hold several tiles); a
                             multiple of 32 up to min(tpb, 512) (Euler 256), else the default */
     int32_t flags;       /* enum sw_flag bits; 0 = none */
 } sw_config;
