@@ -4,8 +4,9 @@
   ``oracle/_build/liboracle.so`` (``-ffp-contract=off``: nothing fused, so the
   oracle keeps the reference's rounding on x86-64 and aarch64 alike).
 * ``build_ref()`` compiles ``ref_harness.cu`` against the reference programs
-  where they lie (``/root/reference/SweptSource``), six times (three problems
-  x float/double), into ``oracle/_ref/libref_<problem>_<f32|f64>.so``.  It runs
+  where they lie (``/root/reference/SweptSource``), eight times (three problems
+  and the KS DIVISE build, x float/double), into
+  ``oracle/_ref/libref_<problem>_<f32|f64>.so`` (``libref_ks_div_*`` for DIVISE).  It runs
   only where the reference sources exist; nothing else reads them.
 """
 from __future__ import annotations
@@ -54,15 +55,19 @@ def reference_available() -> bool:
     return all((REFERENCE_SRC / f).is_file() for f in PROBLEMS.values())
 
 
-def ref_lib_path(problem: int, prec: int) -> Path:
-    return REF_OUT / ("libref_%s_%s.so" % (PROBLEM_NAMES[problem], "f64" if prec == 8 else "f32"))
+def ref_lib_path(problem: int, prec: int, divide: bool = False) -> Path:
+    """divide: the KS DIVISE build's stencil functions (problem 1 only)."""
+    name = PROBLEM_NAMES[problem] + ("_div" if divide else "")
+    return REF_OUT / ("libref_%s_%s.so" % (name, "f64" if prec == 8 else "f32"))
 
 
-def _ref_cmd(problem: int, prec: int, out: Path) -> list[str]:
+def _ref_cmd(problem: int, prec: int, out: Path, divide: bool = False) -> list[str]:
     src = REFERENCE_SRC / PROBLEMS[problem]
     cmd = ["nvcc", "-shared", "-Xcompiler", "-fPIC", "-Xcompiler", "-fopenmp", "-Xcompiler", "-ffp-contract=off",
            "-w", "-O2", "-I", str(REFERENCE_SRC), "-DREF_PROBLEM=%d" % problem,
            '-DREF_SRC="%s"' % src, "-o", str(out), str(HERE / "ref_harness.cu")]
+    if divide:
+        cmd.insert(1, "-DREF_KS_DIVIDE")
     if prec == 8:
         cmd[1:1] = ["-DREAL=double", "-DREALtwo=double2", "-DREALthree=double3", "-DREALfour=double4"]
     return cmd
@@ -74,22 +79,23 @@ def build_ref(force: bool = False) -> list[Path]:
         return []
     REF_OUT.mkdir(exist_ok=True)
     jobs = []
-    for problem in PROBLEMS:
+    variants = [(p, False) for p in PROBLEMS] + [(1, True)]  # + the KS DIVISE build
+    for problem, divide in variants:
         for prec in (4, 8):
-            out = ref_lib_path(problem, prec)
+            out = ref_lib_path(problem, prec, divide)
             if not force and _newer(out, HERE / "ref_harness.cu", REFERENCE_SRC / PROBLEMS[problem]):
                 continue
-            jobs.append((problem, prec, out))
+            jobs.append((problem, prec, out, divide))
 
     def run(job):
-        problem, prec, out = job
-        subprocess.run(_ref_cmd(problem, prec, out), check=True, stdout=subprocess.DEVNULL,
+        problem, prec, out, divide = job
+        subprocess.run(_ref_cmd(problem, prec, out, divide), check=True, stdout=subprocess.DEVNULL,
                        stderr=subprocess.PIPE)
         return out
 
-    with ThreadPoolExecutor(max_workers=6) as ex:
+    with ThreadPoolExecutor(max_workers=8) as ex:
         list(ex.map(run, jobs))
-    return [ref_lib_path(p, q) for p in PROBLEMS for q in (4, 8)]
+    return [ref_lib_path(p, q, d) for p, d in variants for q in (4, 8)]
 
 
 if __name__ == "__main__":

@@ -39,4 +39,5 @@ def golden():
     return {
         "ref": np.load(ROOT / "tests" / "golden" / "ref_classic.npz"),
         "ks": np.load(ROOT / "tests" / "golden" / "ks_official.npz"),
+        "ks_divide": np.load(ROOT / "tests" / "golden" / "ref_ks_divide.npz"),
     }

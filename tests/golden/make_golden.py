@@ -14,6 +14,10 @@ It writes
   ``eulerFinalStep``) compiled host-side from the unmodified reference files
   by ``oracle/ref_harness.cu``; for Euler also the reference's ``pressure`` and
   ``energy`` of that state (the .dat writer's derived rows).
+* ``ref_ks_divide.npz`` -- KS in float and double at dx = 0.3 (divisors that
+  are not powers of two), N classic steps of the reference's DIVISE-build
+  stencil functions (KS1D_SweptShared.cu:111-132, built by the harness with
+  REF_KS_DIVIDE) and of its default reciprocal build, from one seeded IC.
 * ``ks_official.npz`` -- the reference's KS golden run,
   ``SweptSource/Testing/KSDouble_Official.txt`` (nx=1024, dx=0.5, FP64 swept,
   dt=1e-7; Velocity at t = 0, 6, 12, 18, 20), parsed to arrays.
@@ -89,6 +93,27 @@ def make_ref_classic():
     np.savez_compressed(HERE / "ref_classic.npz", **out)
 
 
+def make_ref_ks_divide():
+    obuild.build_ref()
+    nx, dt, dx, nsteps = 256, 5e-4, 0.3, 400
+    out = {"meta": np.array([nx, dt, dx, nsteps], dtype=np.float64)}
+    for prec in (8, 4):
+        dtype = np.float64 if prec == 8 else np.float32
+        x = np.arange(nx)
+        rng = np.random.default_rng(3)
+        ic = (np.cos(2 * np.pi * 5 * x / nx) + 0.1 * rng.standard_normal(nx)).astype(dtype)
+        out["f%d_ic" % (8 * prec)] = ic
+        for divide in (True, False):
+            L = C.CDLL(str(obuild.ref_lib_path(O.KS, prec, divide)))
+            assert L.ref_real_size() == prec
+            c = O.ks_consts(prec, nx, dt, dx=dx, divide=divide)
+            fin = ic.copy()
+            L.ref_classic(C.c_void_p(fin.ctypes.data), C.c_int64(nx), C.c_double(c.dx_times4), C.c_double(c.dx2),
+                          C.c_double(c.dx4), C.c_double(c.dt), C.c_double(c.dt_half), C.c_int64(nsteps))
+            out["f%d_%s" % (8 * prec, "divide" if divide else "multiply")] = fin
+    np.savez_compressed(HERE / "ref_ks_divide.npz", **out)
+
+
 def make_ks_official():
     src = obuild.REFERENCE_SRC / "Testing" / "KSDouble_Official.txt"
     lines = src.read_text().splitlines()
@@ -107,6 +132,7 @@ def make_ks_official():
 
 if __name__ == "__main__":
     make_ref_classic()
+    make_ref_ks_divide()
     make_ks_official()
-    for f in ("ref_classic.npz", "ks_official.npz"):
+    for f in ("ref_classic.npz", "ref_ks_divide.npz", "ks_official.npz"):
         print(f, (HERE / f).stat().st_size, "bytes")

@@ -35,6 +35,21 @@ def test_classic_is_reference_bit_exact(oracle, golden, name, bits):
 
 
 @pytest.mark.parametrize("bits", [64, 32])
+def test_ks_divide_is_reference_bit_exact(oracle, golden, bits):
+    """The oracle's divide form == the reference's DIVISE-build stencil functions
+    (KS1D_SweptShared.cu:111-132) at dx = 0.3, bit for bit; and its reciprocal
+    form == the reference's default build there, which rounds differently."""
+    g = golden["ks_divide"]
+    nx, dt, dx, nsteps = g["meta"]
+    prec = bits // 8
+    for divide, key in ((True, "divide"), (False, "multiply")):
+        c = oracle.ks_consts(prec, int(nx), dt, dx=dx, divide=divide)
+        out = oracle.classic(c, g["f%d_ic" % bits], int(nsteps))
+        np.testing.assert_array_equal(out, g["f%d_%s" % (bits, key)])
+    assert not np.array_equal(g["f%d_divide" % bits], g["f%d_multiply" % bits])
+
+
+@pytest.mark.parametrize("bits", [64, 32])
 def test_euler_pressure_is_reference(oracle, golden, bits):
     """The .dat Pressure row: oracle pressure() == the reference's pressure()."""
     key = "euler_f%d" % bits
