@@ -288,6 +288,7 @@ def run_ours(args) -> None:
             "achieved": achieved, "peak": hbm,
             "unit": "GB/s", "frac": achieved / hbm, "peak_source": peak_src,
             "traffic": DIAMOND_TRAFFIC_BYTES, "traffic_source": "ncu dram__bytes_read+write, one diamond launch",
+            "traffic_gbs": DIAMOND_TRAFFIC_BYTES / (launch_ms * 1e-3) / 1e9,
             "launch_ms": launch_ms,
             "algorithmic_bytes_per_launch": alg_bytes,
             "note": "effective bandwidth: classic KS FP64 bytes (40 B/cell-update) x cells x 32 steps per "
