@@ -10,6 +10,7 @@
  *   Heat  : execFunc + classicHeat          SweptSource/Heat1D_SweptShared.cu:121-145
  *   KS    : convect/secondDer/fourthDer,
  *           stutterStep/finalStep/classicKS SweptSource/KS1D_SweptShared.cu:136-207
+ *           (and the DIVISE build's forms,  :111-132, with or_consts.divide)
  *   Euler : pressure ... eulerFinalStep,
  *           classicEuler                    SweptSource/Euler1D_SweptShared.cu:183-426
  * in the reference's own operation order, compiled with -ffp-contract=off so
