@@ -63,6 +63,26 @@ def test_struct_layouts_match_header(sw, tmp_path):
             assert int(got["%s.%s" % (cname, f)]) == getattr(py, f).offset, (cname, f)
 
 
+def test_enum_values_match_header(sw, tmp_path):
+    """The Python binding's enum constants equal the header's."""
+    from importlib import import_module
+    native = import_module("1dsweptcuda_gb300.native")
+    names = {"SW_HEAT": native.HEAT, "SW_KS": native.KS, "SW_EULER": native.EULER,
+             "SW_ALG_CLASSIC": native.ALG_CLASSIC, "SW_ALG_SWEPT": native.ALG_SWEPT,
+             "SW_ALG_VARIANT": native.ALG_VARIANT, "SW_ALG_SELFTEST": native.ALG_SELFTEST,
+             "SW_BC_DEFAULT": native.BC_DEFAULT, "SW_BC_MIRROR": native.BC_MIRROR,
+             "SW_BC_PERIODIC": native.BC_PERIODIC, "SW_BC_DIRICHLET": native.BC_DIRICHLET,
+             "SW_TIME_REFERENCE": native.TIME_REFERENCE, "SW_TIME_STEPS": native.TIME_STEPS,
+             "SW_FLAG_KS_DIVIDE": native.FLAG_KS_DIVIDE}
+    src = tmp_path / "e.c"
+    src.write_text("\n".join(['#include <stdio.h>', '#include "swept1d.h"', "int main(void){"] +
+                              ['printf("%s %%d\\n", (int)%s);' % (n, n) for n in names] + ["return 0;}"]))
+    exe = tmp_path / "e"
+    subprocess.run(["gcc", "-I", str(ROOT / "include"), "-o", str(exe), str(src)], check=True)
+    got = dict(ln.split() for ln in subprocess.run([str(exe)], capture_output=True, text=True).stdout.splitlines())
+    assert {k: int(v) for k, v in got.items()} == names
+
+
 def test_strerror_and_version(sw):
     lib = sw.library()
     assert lib.sw_abi_version() == 1
