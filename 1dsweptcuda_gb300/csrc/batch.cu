@@ -27,14 +27,35 @@ bool valid_tile(int W, int32_t n, const int64_t *nx) {
     return true;
 }
 
+// The checks sw_validate makes of one run, made for every domain: the
+// problem's boundary condition and flags, and for Euler its stability limit.
+// Every domain shares one set of constants (the kernels take one Params), so
+// an Euler ensemble of uneven lengths must give dx: the reference's default
+// dx = 1/(nx-2) would differ from domain to domain.
 int check_batch(const sw_config *c, int32_t n, const int64_t *nx) {
     if (!c || !nx || n < 1) return SW_ERR_ARG;
     if (c->problem < SW_HEAT || c->problem > SW_EULER || (c->precision != 4 && c->precision != 8)) return SW_ERR_ARG;
     if (c->alg < SW_ALG_CLASSIC || c->alg > SW_ALG_VARIANT) return SW_ERR_ARG;
-    if (c->time_mode != SW_TIME_STEPS || c->n_steps < 0 || !(c->dt > 0)) return SW_ERR_ARG;
+    if (c->time_mode != SW_TIME_STEPS || c->n_steps < 0 || !(c->dt > 0) || !std::isfinite(c->dt)) return SW_ERR_ARG;
+    if ((c->flags & ~SW_FLAG_KS_DIVIDE) != 0) return SW_ERR_ARG;
+    if ((c->flags & SW_FLAG_KS_DIVIDE) && c->problem != SW_KS) return SW_ERR_ARG;
+    const int bc = resolved_bc(*c);
+    if (c->problem == SW_HEAT && bc != SW_BC_MIRROR && bc != SW_BC_PERIODIC) return SW_ERR_ARG;
+    if (c->problem == SW_KS && bc != SW_BC_PERIODIC) return SW_ERR_ARG;
+    if (c->problem == SW_EULER && bc != SW_BC_DIRICHLET) return SW_ERR_ARG;
     for (int32_t d = 0; d < n; ++d)
         if (nx[d] < 32 || nx[d] > ((int64_t)1 << 34)) return SW_ERR_SIZE;
     if (c->tpb != 0 && c->alg != SW_ALG_CLASSIC && !valid_tile(c->tpb, n, nx)) return SW_ERR_SIZE;
+    if (c->problem == SW_EULER) {
+        if (c->dx == 0)
+            for (int32_t d = 1; d < n; ++d)
+                if (nx[d] != nx[0]) return SW_ERR_ARG;
+        sw_config one = *c;
+        one.nx = nx[0];
+        sw_constants k;
+        sw_constants_of(&one, &k);
+        if (k.dt_dx > 0.21) return SW_ERR_UNSTABLE;  // Euler1D_SweptShared.cu:1168-1172
+    }
     return SW_OK;
 }
 

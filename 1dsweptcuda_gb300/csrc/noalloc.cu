@@ -26,14 +26,23 @@ void *g_scratch[kMaxDevices] = {};
 
 // Device address of the scratch array on the current device.  In host code
 // the array's name is only a host-side stand-in, so the address is asked from
-// the runtime once per device (the first call on that device).
-cudaError_t scratch_address(void **out) {
+// the runtime.  It is asked again on every call made outside stream capture
+// (a cheap lookup once the module is loaded), so a context that the host
+// application destroyed and re-created (cudaDeviceReset) is never left with
+// a stale address; inside a capture the address of the last call outside one
+// is used, which is why the first call on a device must come before any
+// capture.
+cudaError_t scratch_address(cudaStream_t s, void **out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    e = cudaStreamIsCapturing(s, &cap);
+    if (e != cudaSuccess) return e;
     std::lock_guard<std::mutex> lock(g_setup_lock);
-    if (!g_scratch[dev]) {
+    if (cap == cudaStreamCaptureStatusNone || !g_scratch[dev]) {
+        if (cap != cudaStreamCaptureStatusNone) return cudaErrorStreamCaptureUnsupported;
         void *p = nullptr;
         e = cudaGetSymbolAddress(&p, sw_noalloc_scratch);
         if (e != cudaSuccess) return e;
@@ -43,16 +52,31 @@ cudaError_t scratch_address(void **out) {
     return cudaSuccess;
 }
 
+// The state must be device memory of the current device: the scratch array
+// used is the current device's, and a kernel must not read another GPU's
+// memory through it.
+bool on_current_device(const void *state) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return false;
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, state) != cudaSuccess) {
+        cudaGetLastError();  // an unregistered host pointer may leave an error behind
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice && a.device == dev;
+}
+
+// Scratch bytes a run needs: the slots (two cells per cell) and one work row.
+size_t scratch_need(const Ops *ops, int64_t nx) { return ops->cell * (size_t)nx * 3; }
+
 template <typename T>
 int run(const sw_config &c, void *state, cudaStream_t s) {
     const Ops *ops = ops_for(c.problem, c.precision, c.flags);
     const int W = c.tpb;
     const int64_t nx = c.nx;
     const size_t slot_bytes = ops->cell * (size_t)nx * 2;
-    const size_t need = slot_bytes + ops->cell * (size_t)nx;
-    if (need > (size_t)SW_NOALLOC_SCRATCH_BYTES) return SW_ERR_SIZE;
     void *scratch = nullptr;
-    if (scratch_address(&scratch) != cudaSuccess) return SW_ERR_CUDA;
+    if (scratch_address(s, &scratch) != cudaSuccess) return SW_ERR_CUDA;
     void *slots = scratch;
     void *work = static_cast<char *>(scratch) + slot_bytes;
 
@@ -90,6 +114,9 @@ extern "C" int sw_run_device_noalloc(const sw_config *cfg, void *state_dev, void
     int rc = sw_validate(cfg);
     if (rc) return rc;
     if (cfg->alg != SW_ALG_SWEPT || cfg->time_mode != SW_TIME_STEPS) return SW_ERR_UNSUPPORTED;
+    if (scratch_need(ops_for(cfg->problem, cfg->precision, cfg->flags), cfg->nx) > (size_t)SW_NOALLOC_SCRATCH_BYTES)
+        return SW_ERR_SIZE;
+    if (!on_current_device(state_dev)) return SW_ERR_ARG;
     if (cfg->precision == 4) return run<float>(*cfg, state_dev, (cudaStream_t)stream);
     return run<double>(*cfg, state_dev, (cudaStream_t)stream);
 }

@@ -30,7 +30,8 @@ EXPORTED = ["sw_abi_version", "sw_strerror", "sw_ctx_create", "sw_ctx_destroy", 
             "sw_config_init", "sw_validate", "sw_constants_of", "sw_initial_condition", "sw_run",
             "sw_run_device", "sw_plan", "sw_cli_main", "sw_run_batch", "sw_run_batch_device",
             "sw_query_tuning", "sw_run_device_noalloc", "sw_closure_infer", "sw_closure_step",
-            "sw_closure_grad", "sw_closure_adam", "sw_closure_train", "sw_coarse_grain", "sw_wait_probe"]
+            "sw_closure_grad", "sw_closure_adam", "sw_closure_train", "sw_coarse_grain", "sw_wait_probe",
+            "sw_fp64_rates"]
 CLOSURE_PARAMS = 5506
 NOALLOC_SCRATCH_BYTES = 24 * 1024 * 1024
 
@@ -135,10 +136,13 @@ def library():
                                    C.c_uint64, C.POINTER(C.c_float)]
     L.sw_coarse_grain.argtypes = [vp, vp, vp, C.c_int64, C.c_int32]
     L.sw_wait_probe.argtypes = [vp, C.c_int64, C.POINTER(C.c_double)]
+    dp = C.POINTER(C.c_double)
+    L.sw_fp64_rates.argtypes = [vp, dp, dp, dp]
     for name in ("sw_ctx_create", "sw_ctx_destroy", "sw_config_init", "sw_validate", "sw_constants_of",
                  "sw_initial_condition", "sw_run", "sw_run_device", "sw_cli_main", "sw_plan", "sw_run_batch",
                  "sw_run_batch_device", "sw_query_tuning", "sw_run_device_noalloc", "sw_closure_infer",
-                 "sw_closure_step", "sw_closure_grad", "sw_closure_adam", "sw_closure_train", "sw_coarse_grain"):
+                 "sw_closure_step", "sw_closure_grad", "sw_closure_adam", "sw_closure_train", "sw_coarse_grain",
+                 "sw_fp64_rates"):
         getattr(L, name).restype = C.c_int
     _lib = L
     return L
@@ -302,7 +306,16 @@ class _BatchMixin:
         return rc, ms.value
 
 
-for _name in ("run_batch", "run_batch_device", "tune", "wait_probe"):
+    def fp64_rates(self) -> dict:
+        """sw_fp64_rates: measured FP64 fma / add / multiply issue rates (operations/s)."""
+        f, a, m = C.c_double(), C.c_double(), C.c_double()
+        rc = self._lib.sw_fp64_rates(self._ctx, C.byref(f), C.byref(a), C.byref(m))
+        if rc:
+            raise self._err(rc, "sw_fp64_rates")
+        return {"fma": f.value, "add": a.value, "mul": m.value}
+
+
+for _name in ("run_batch", "run_batch_device", "tune", "wait_probe", "fp64_rates"):
     setattr(Solver, _name, getattr(_BatchMixin, _name))
 
 

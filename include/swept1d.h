@@ -275,12 +275,17 @@ int sw_coarse_grain(sw_ctx *ctx, const double *fine, float *coarse, int64_t n_co
  * (e.g. up to nx = 2^20 for FP64 Heat/KS, 2^18 for FP64 Euler).  It calls no
  * cudaMalloc, cudaFree or other allocating routine.
  *
- * The first call on a device looks up the array's device address
- * (cudaGetSymbolAddress); make that first call before any stream capture.
- * Every call on a device shares the one array and leaves its contents behind
- * (nothing in it needs to start at zero); calls that overlap on the GPU --
- * on different streams, or from different host threads -- race on it, so
- * order them on one stream. */
+ * state_dev must be device memory of the CUDA device that is current when
+ * the call is made (the array used is that device's); anything else returns
+ * SW_ERR_ARG.  The array's device address is looked up (cudaGetSymbolAddress)
+ * on every call made outside stream capture, so a device reset by the host
+ * application is picked up by the next such call; a call inside a capture
+ * reuses the address found by the last call outside one, so make the first
+ * call on a device, and the first after a device reset, before any stream
+ * capture.  Every call on a device shares the one array and leaves its
+ * contents behind (nothing in it needs to start at zero); calls that overlap
+ * on the GPU -- on different streams, or from different host threads -- race
+ * on it, so order them on one stream. */
 #define SW_NOALLOC_SCRATCH_BYTES (24u * 1024u * 1024u)
 int sw_run_device_noalloc(const sw_config *cfg, void *state_dev, void *stream);
 
@@ -289,6 +294,13 @@ int sw_run_device_noalloc(const sw_config *cfg, void *state_dev, void *stream);
  * (1e6..1e10 ns).  Returns SW_ERR_TIMEOUT once the wait has run out, with the
  * wait's duration in *waited_ms (may be NULL); the context stays usable. */
 int sw_wait_probe(sw_ctx *ctx, int64_t limit_ns, double *waited_ms);
+
+/* Measurement aid (no reference counterpart): the FP64 pipe's issue rates
+ * of the context's device, in operations per second, measured with a full
+ * grid of independent fma / add / multiply chains (about 0.3 s).  The swept
+ * and classic FP64 kernels are bound by this pipe, not by HBM; their roofs
+ * are these rates times each stencil's operation counts. */
+int sw_fp64_rates(sw_ctx *ctx, double *fma_per_s, double *add_per_s, double *mul_per_s);
 
 /* The whole program: argv exactly as bin/<Problem><Precision>Out takes it
  * (replaces main(), Heat1D_SweptShared.cu:697-836, KS1D_SweptShared.cu:866-1029,

@@ -4,10 +4,14 @@
   ``oracle/_build/liboracle.so`` (``-ffp-contract=off``: nothing fused, so the
   oracle keeps the reference's rounding on x86-64 and aarch64 alike).
 * ``build_ref()`` compiles ``ref_harness.cu`` against the reference programs
-  where they lie (``/root/reference/SweptSource``), eight times (three problems
+  where they lie, eight times (three problems
   and the KS DIVISE build, x float/double), into
   ``oracle/_ref/libref_<problem>_<f32|f64>.so`` (``libref_ks_div_*`` for DIVISE).  It runs
   only where the reference sources exist; nothing else reads them.
+
+The reference's ``SweptSource`` folder is taken from ``SWEPT1D_REFERENCE_SRC``
+when that is set, else from a checkout of the reference named ``reference``
+beside this repository's folder (``../reference/SweptSource``).
 """
 from __future__ import annotations
 
@@ -20,7 +24,7 @@ from pathlib import Path
 HERE = Path(__file__).resolve().parent
 BUILD = HERE / "_build"
 REF_OUT = HERE / "_ref"
-REFERENCE_SRC = Path(os.environ.get("SWEPT1D_REFERENCE_SRC", "/root/reference/SweptSource"))
+REFERENCE_SRC = Path(os.environ.get("SWEPT1D_REFERENCE_SRC") or HERE.parent.parent / "reference" / "SweptSource")
 
 PROBLEMS = {0: "Heat1D_SweptShared.cu", 1: "KS1D_SweptShared.cu", 2: "Euler1D_SweptShared.cu"}
 PROBLEM_NAMES = {0: "heat", 1: "ks", 2: "euler"}

@@ -1,7 +1,8 @@
 """Generate the golden fixtures in this folder from the reference itself.
 
-Run in a checkout where the reference sources exist (default
-/root/reference/SweptSource, override with SWEPT1D_REFERENCE_SRC):
+Run in a checkout where the reference sources exist (SWEPT1D_REFERENCE_SRC, or
+by default a checkout named ``reference`` beside this repository's folder,
+``../reference/SweptSource``):
 
     python tests/golden/make_golden.py
 

@@ -19,7 +19,7 @@ HEADER = ROOT / "include" / "swept1d.h"
 def declared_functions():
     text = HEADER.read_text()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return sorted(set(re.findall(r"\b(sw_[a-z_]+)\s*\(", text)))
+    return sorted(set(re.findall(r"\b(sw_[a-z0-9_]+)\s*\(", text)))
 
 
 def test_library_exports_every_declared_function(sw):

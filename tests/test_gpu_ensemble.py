@@ -85,3 +85,25 @@ def test_ensemble_rejects_bad_tile(sw, solver):
     with pytest.raises(sw.NativeError) as e:
         solver.run_batch(cfg, nx, np.zeros(int(nx.sum())))
     assert e.value.code == -2
+
+
+def test_ensemble_applies_the_single_run_checks_to_every_domain(sw, solver):
+    """sw_validate's checks hold for ensembles too: an Euler ensemble of uneven
+    lengths must state dx (the default 1/(nx-2) differs per domain), Euler's
+    stability limit applies, and the problem's boundary condition and flags
+    are checked -- each rejected before any launch."""
+    nx = np.array([256, 512], dtype=np.int64)
+    ic = np.zeros(int(nx.sum()) * 3)
+    cases = [
+        (dict(problem=2, dt=1e-5), -1),                     # uneven Euler lengths, dx from nx: refused
+        (dict(problem=2, dt=0.5 / 254, dx=1.0 / 254), -3),  # dt/dx = 0.5 > 0.21: unstable
+        (dict(problem=1, bc=sw.BC_MIRROR, dt=0.005), -1),   # KS is periodic only
+        (dict(problem=0, flags=sw.FLAG_KS_DIVIDE, dt=0.004), -1),  # the divide flag is KS's
+    ]
+    for over, code in cases:
+        problem = over.pop("problem")
+        cfg = sw.make_config(problem, 8, alg=1, tpb=64, time_mode=sw.TIME_STEPS, n_steps=8, **over)
+        state = ic if problem == 2 else np.zeros(int(nx.sum()))
+        with pytest.raises(sw.NativeError) as e:
+            solver.run_batch(cfg, nx, state)
+        assert e.value.code == code, (problem, over)

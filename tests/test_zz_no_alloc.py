@@ -27,17 +27,21 @@ def _device_ic(sw, cfg):
     return ic
 
 
-@pytest.mark.parametrize("problem,prec,nx,tpb,dt,steps", [
-    (1, 8, 1 << 20, 256, 0.005, 200),        # the benchmark's KS domain, the largest FP64 size the scratch holds
-    (1, 4, 1 << 16, 128, 0.005, 101),        # remainder steps use the scratch work row
-    (0, 8, 4096, 128, 0.004, 333),           # Heat: odd remainder ends in the work row
-    (2, 8, 1 << 14, 256, 0.1 / 16382, 97),   # Euler, 4 values per cell
+@pytest.mark.parametrize("problem,prec,nx,tpb,dt,steps,threads", [
+    (1, 8, 1 << 20, 256, 0.005, 200, 0),      # the benchmark's KS domain, the largest FP64 size the scratch holds
+    (1, 4, 1 << 16, 128, 0.005, 101, 0),      # remainder steps use the scratch work row
+    (0, 8, 4096, 128, 0.004, 333, 0),         # Heat: odd remainder ends in the work row
+    (2, 8, 1 << 14, 256, 0.1 / 16382, 97, 0),  # Euler, 4 values per cell
+    (1, 4, 1 << 20, 1024, 0.005, 515, 0),     # FP32 KS, 1024 tiles of 1024 cells, 4 cells per thread
+    (1, 4, 1 << 18, 256, 0.005, 203, 0),      # FP32 KS, 1024 tiles: four tiles per block (grouped slots)
+    (1, 8, 1 << 16, 256, 0.005, 131, 128),    # a non-default threads per block: two cells per thread
 ])
-def test_noalloc_matches_sw_run_device_twice(sw, solver, problem, prec, nx, tpb, dt, steps):
+def test_noalloc_matches_sw_run_device_twice(sw, solver, problem, prec, nx, tpb, dt, steps, threads):
     torch = pytest.importorskip("torch")
     lib = sw.library()
     cfg = sw.make_config(problem, prec, alg=sw.ALG_SWEPT, nx=nx, tpb=tpb, dt=dt, time_mode=sw.TIME_STEPS,
                          n_steps=steps)
+    cfg.threads = threads
     ic = _device_ic(sw, cfg)
     want = torch.from_numpy(ic.copy()).cuda()
     solver.run_device(cfg, want.data_ptr())
@@ -64,3 +68,12 @@ def test_noalloc_rejects_sizes_beyond_the_scratch(sw):
     classic = sw.make_config(1, 8, alg=sw.ALG_CLASSIC, nx=1024, tpb=256, dt=0.005, time_mode=sw.TIME_STEPS,
                              n_steps=32)
     assert lib.sw_run_device_noalloc(C.byref(classic), C.c_void_p(1), None) == -8  # swept only
+
+
+def test_noalloc_rejects_a_state_that_is_not_device_memory(sw):
+    """A host buffer (or any pointer that is not device memory of the current
+    device) is turned away before a kernel could touch it."""
+    lib = sw.library()
+    cfg = sw.make_config(1, 8, alg=sw.ALG_SWEPT, nx=1024, tpb=256, dt=0.005, time_mode=sw.TIME_STEPS, n_steps=32)
+    host = np.zeros(1024, dtype=np.float64)
+    assert lib.sw_run_device_noalloc(C.byref(cfg), host.ctypes.data_as(C.c_void_p), None) == -1  # SW_ERR_ARG
