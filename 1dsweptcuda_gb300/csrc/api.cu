@@ -627,4 +627,28 @@ int sw_run_device(sw_ctx *ctx, const sw_config *cfg, void *state_dev, void *stre
     return run_any(ctx, cfg, nullptr, nullptr, state_dev, stream, nullptr, nullptr, out);
 }
 
+int sw_swept_pass(sw_ctx *ctx, const sw_config *cfg, int32_t mode, int32_t phase, void *state_dev, void *slots_dev,
+                  void *stream) {
+    if (!ctx || !cfg) return SW_ERR_ARG;
+    int rc = sw_validate(cfg);
+    if (rc) return fail(ctx, rc, std::string("invalid configuration: ") + sw_strerror(rc));
+    if (cfg->alg != SW_ALG_SWEPT) return fail(ctx, SW_ERR_UNSUPPORTED, "a swept pass needs alg 1");
+    if (mode < MODE_UP || mode > MODE_DOWN || (phase != 0 && phase != 1) || (mode == MODE_UP && phase != 0))
+        return fail(ctx, SW_ERR_ARG, "mode must be 0 (up, phase 0), 1 (diamond) or 2 (down); phase 0 or 1");
+    if (!state_dev || !slots_dev) return fail(ctx, SW_ERR_ARG, "null device state or slots");
+    const Ops *ops = ops_for(cfg->problem, cfg->precision, cfg->flags);
+    SW_CUDA(ctx, cudaSetDevice(ctx->device));
+    sw_constants k;
+    sw_constants_of(cfg, &k);
+    cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+    if (cfg->precision == 4) {
+        const Params<float> p = make_params<float>(*cfg, k);
+        SW_CUDA(ctx, ops->swept(&p, mode, phase, state_dev, slots_dev, cfg->nx, cfg->tpb, cfg->threads, s));
+    } else {
+        const Params<double> p = make_params<double>(*cfg, k);
+        SW_CUDA(ctx, ops->swept(&p, mode, phase, state_dev, slots_dev, cfg->nx, cfg->tpb, cfg->threads, s));
+    }
+    return SW_OK;
+}
+
 }  // extern "C"

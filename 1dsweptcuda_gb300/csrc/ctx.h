@@ -86,6 +86,11 @@ inline Params<T> make_params(const sw_config &c, const sw_constants &k) {
     if (c.problem == SW_KS && (c.flags & SW_FLAG_KS_DIVIDE)) p.ks_form = KS_DIVIDE;
     else if (c.problem == SW_KS && is_pow2(p.c4) && is_pow2(p.d2) && is_pow2(p.d4)) p.ks_form = KS_POW2;
     else p.ks_form = KS_MULTIPLY;
+    if (p.ks_form == KS_POW2) {
+        int e = 0;
+        std::frexp((double)p.d2, &e);  // d2 = 0.5 * 2^e
+        p.d2_e = e - 1;
+    }
     return p;
 }
 

@@ -134,9 +134,14 @@ __device__ __forceinline__ void tile_point(const Params<T> &p, T *rows, int L, i
     }
 }
 
+// Euler tiles also keep, per level, the interface terms of euler_level_tile:
+// the pressure differences D and the flux F and dissipation S (3 components
+// each) of every interface, 7 values per row position.
+constexpr int kEulerIfaceArrays = 7;
 template <int P, typename T>
 __host__ __device__ constexpr size_t swept_smem_bytes(int W) {
-    return sizeof(T) * tile_rows<P>() * Scheme<P, T>::C * (size_t)row_stride(W);
+    return sizeof(T) * ((size_t)tile_rows<P>() * Scheme<P, T>::C + (P == SW_EULER ? kEulerIfaceArrays : 0)) *
+           (size_t)row_stride(W);
 }
 
 __device__ __forceinline__ int64_t wrap_pos(int64_t q, int64_t nx) {
@@ -344,6 +349,61 @@ __device__ __forceinline__ void euler_level(const Params<T> &p, T *rows, int L, 
     }
 }
 
+// Euler sub-step over tile cells [lo, hi) of a swept tile, every interface
+// computed once, in three passes of the whole block through shared memory
+// (xs: kEulerIfaceArrays rows of L values after the tile rows):
+//   A. the pressure-difference numerator D_k of each neighbour pair (k-1, k),
+//      k in [lo-1, hi+2) -- zero across the domain's ends (the reference's
+//      edge flags, Euler1D_SweptShared.cu:311-335);
+//   B. the flux F_b and dissipation S_b of each interface (b-1, b), b in
+//      [lo, hi+1), from the four cells around it and D_{b-1}, D_b, D_{b+1};
+//   C. each cell's update from its two interfaces (eu_combine).
+// Same operations on the same values as euler_level (and so as the
+// reference's per-cell form), but every lane of pass B computes an interface
+// that is used: euler_level's 29-cell warps spend 3 lanes of 32 on terms only
+// their neighbours need.  The cells read lie in [lo-2, hi+1], inside the row
+// and its margins, as for euler_level.
+template <typename T>
+__device__ __forceinline__ void euler_level_tile(const Params<T> &p, T *rows, int L, int par, int lo, int hi, Ends e) {
+    constexpr int R = Scheme<SW_EULER, T>::R;
+    const T *src = rows + (par ^ 1) * 3 * L + R;
+    T *dst = rows + par * 3 * L + R;
+    T *D = rows + 6 * L + R;  // D[k], F[c * L + b], S[c * L + b] at tile position k, b
+    T *F = D + L, *S = D + 4 * L;
+    const int t0 = (int)threadIdx.x, nt = (int)blockDim.x;
+    for (int k = lo - 1 + t0; k < hi + 2; k += nt) {
+        const Q3<T> a = q3(src[k - 1], src[L + k - 1], src[2 * L + k - 1]);
+        const Q3<T> b = q3(src[k], src[L + k], src[2 * L + k]);
+        D[k] = (k == e.first || k - 1 == e.last) ? T(0) : eu_pdiff(a, b);
+    }
+    __syncthreads();
+    for (int b = lo + t0; b < hi + 1; b += nt) {
+        Q3<T> c[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) c[k] = q3(src[b - 2 + k], src[L + b - 2 + k], src[2 * L + b - 2 + k]);
+        Q3<T> f, g;
+        eu_iface(p, c[0], c[1], c[2], c[3], D[b - 1], D[b], D[b + 1], f, g);
+        F[b] = f.x;
+        F[L + b] = f.y;
+        F[2 * L + b] = f.z;
+        S[b] = g.x;
+        S[L + b] = g.y;
+        S[2 * L + b] = g.z;
+    }
+    __syncthreads();
+    const T scale = par ? ml(T(0.25), p.dtdx) : ml(T(0.5), p.dtdx);
+    for (int b = lo + t0; b < hi; b += nt) {
+        if (b == e.first || b == e.last) continue;
+        const Q3<T> fl = q3(F[b], F[L + b], F[2 * L + b]), sl = q3(S[b], S[L + b], S[2 * L + b]);
+        const Q3<T> fr = q3(F[b + 1], F[L + b + 1], F[2 * L + b + 1]), sr = q3(S[b + 1], S[L + b + 1], S[2 * L + b + 1]);
+        const Q3<T> base = par ? q3(src[b], src[L + b], src[2 * L + b]) : q3(dst[b], dst[L + b], dst[2 * L + b]);
+        const Q3<T> o = qadd(base, qscale(scale, eu_combine(fl, sl, fr, sr)));
+        dst[b] = o.x;
+        dst[L + b] = o.y;
+        dst[2 * L + b] = o.z;
+    }
+}
+
 // Which cell mapping a kernel carries: PATH_ANY picks at run time (blockDim.x
 // * 4 == W: 4 cells per thread), PATH_CELL and PATH_SPAN4 hold only one, so a
 // kernel does not pay the registers of a path it never runs.  Euler always
@@ -369,7 +429,7 @@ template <int P, typename T, int PATH>
 __device__ __forceinline__ void tile_level(const Params<T> &p, T *rows, int L, int W, int par, int lo, int hi,
                                            Ends e) {
     if constexpr (P == SW_EULER) {
-        euler_level<T>(p, rows, L, W, par, lo, hi, e);
+        euler_level_tile<T>(p, rows, L, par, lo, hi, e);
     } else if constexpr (PATH == PATH_SPAN4) {
         tile_span4<P, T>(p, rows, L, par, lo, hi, e, (int)threadIdx.x);
     } else if constexpr (PATH == PATH_CELL) {
@@ -484,8 +544,15 @@ __device__ __forceinline__ void swept_tile(const Params<T> &p, typename Scheme<P
 
 // One swept pass over all tiles of one domain; block = one tile.
 // FP32 four-cells-per-thread blocks ask for 2048 resident threads per SM (32 registers).
+// Euler tiles (256 threads) ask for SW_EULER_MIN_BLOCKS blocks per SM: an
+// Euler level is three passes with a barrier after each, and other blocks'
+// warps keep the FP64 pipe busy through them.
+#ifndef SW_EULER_MIN_BLOCKS
+#define SW_EULER_MIN_BLOCKS 4
+#endif
 template <int P, typename T, int PATH>
 constexpr int swept_min_blocks() {
+    if (P == SW_EULER) return SW_EULER_MIN_BLOCKS;
     return (PATH == PATH_SPAN4 && sizeof(T) == 4) ? 2048 / Scheme<P, T>::MAXT : 1;
 }
 template <int P, typename T, int MODE, int PATH>
@@ -633,12 +700,26 @@ __device__ __forceinline__ int group_slot(int t, int n) {
     for (int q = 1; q < G; ++q) k += (t >= q * n) ? 1 : 0;
     return k;
 }
+// SW_GROUP_ROTATE: a level's packed cells start at warp `rot` (mod the
+// block's warps) instead of warp 0, rot = (level + block) mod 4.  A warp's SM
+// sub-partition is its index mod 4, so a level's last, part-filled warp then
+// lands on a different sub-partition from level to level and from block to
+// block, instead of always on the first.
+#ifndef SW_GROUP_ROTATE
+#define SW_GROUP_ROTATE 0
+#endif
 template <int P, typename T, int G, int PATH>
 __device__ __forceinline__ void group_level(const Params<T> &p, T *rows, int TS, int L, int par, int lo, int hi,
-                                            const Ends (&e)[G]) {
+                                            const Ends (&e)[G], int level) {
     // threads per tile at this level
     const int n = (PATH == PATH_SPAN4) ? ((hi - (lo & ~3) + 3) >> 2) : (hi - lo);
+#if SW_GROUP_ROTATE
+    int t = (int)threadIdx.x - 32 * ((level + (int)blockIdx.x) & 3);
+    if (t < 0) t += (int)blockDim.x;
+#else
     const int t = (int)threadIdx.x;
+    (void)level;
+#endif
     if (t < G * n) {
         const int k = group_slot<G>(t, n);
         Ends ek = e[0];
@@ -675,9 +756,9 @@ __device__ __forceinline__ void swept_tile_group(const Params<T> &p, T *__restri
     __syncthreads();
     if constexpr (MODE != MODE_UP) {  // down part, two levels per iteration (H is even)
         for (int j = 1; j < H; j += 2) {
-            group_level<P, T, G, PATH>(p, rows, TS, L, 1, h - j * R, h + j * R, e);
+            group_level<P, T, G, PATH>(p, rows, TS, L, 1, h - j * R, h + j * R, e, j);
             __syncthreads();
-            group_level<P, T, G, PATH>(p, rows, TS, L, 0, h - (j + 1) * R, h + (j + 1) * R, e);
+            group_level<P, T, G, PATH>(p, rows, TS, L, 0, h - (j + 1) * R, h + (j + 1) * R, e, j + 1);
             __syncthreads();
         }
     }
@@ -689,12 +770,12 @@ __device__ __forceinline__ void swept_tile_group(const Params<T> &p, T *__restri
     } else {
         int u = 1;
         for (; u + 1 < H; u += 2) {
-            group_level<P, T, G, PATH>(p, rows, TS, L, 1, u * R, W - u * R, e);
+            group_level<P, T, G, PATH>(p, rows, TS, L, 1, u * R, W - u * R, e, u);
             __syncthreads();
-            group_level<P, T, G, PATH>(p, rows, TS, L, 0, (u + 1) * R, W - (u + 1) * R, e);
+            group_level<P, T, G, PATH>(p, rows, TS, L, 0, (u + 1) * R, W - (u + 1) * R, e, u + 1);
             __syncthreads();
         }
-        group_level<P, T, G, PATH>(p, rows, TS, L, 1, u * R, W - u * R, e);  // u = H - 1
+        group_level<P, T, G, PATH>(p, rows, TS, L, 1, u * R, W - u * R, e, u);  // u = H - 1
         __syncthreads();
         for (int i = threadIdx.x; i < G * W; i += blockDim.x) {
             const int k = i / W, x = i - k * W;
@@ -703,8 +784,10 @@ __device__ __forceinline__ void swept_tile_group(const Params<T> &p, T *__restri
     }
 }
 
+// Two 1024-thread blocks per SM (32 registers): the FP64 levels need the
+// warps of both to keep the FP64 pipe fed across each level's barrier.
 template <int P, typename T, int MODE, int G, int PATH>
-__global__ void __launch_bounds__(1024) k_swept_group(const Params<T> p, T *__restrict__ state,
+__global__ void __launch_bounds__(1024, 2) k_swept_group(const Params<T> p, T *__restrict__ state,
                                                       T *__restrict__ slots, const int W, const int phase) {
     extern __shared__ __align__(16) unsigned char sw_smem[];
     swept_tile_group<P, T, MODE, G, PATH>(p, state, slots, reinterpret_cast<T *>(sw_smem), W, phase,
@@ -925,10 +1008,12 @@ cudaError_t launch_swept(const void *vp, int mode, int phase, void *state, void 
         const int64_t ntiles = nx / W;
         const bool group = threads_req == 0 && ntiles >= kGroupMinTiles;
         if (threads * 4 == W) {
-            if (group && W <= 256 && P == SW_KS && ntiles % 4 == 0)
-                return launch_swept_group<P, T, 4, PATH_SPAN4>(p, mode, phase, st, sl, nx, W, threads, s);
-            if (group && W <= 256 && ntiles % 2 == 0)
-                return launch_swept_group<P, T, 2, PATH_SPAN4>(p, mode, phase, st, sl, nx, W, threads, s);
+            if constexpr (sizeof(T) == 4) {  // FP64 defaults to a cell per thread: no grouped 4-cell kernels
+                if (group && W <= 256 && P == SW_KS && ntiles % 4 == 0)
+                    return launch_swept_group<P, T, 4, PATH_SPAN4>(p, mode, phase, st, sl, nx, W, threads, s);
+                if (group && W <= 256 && ntiles % 2 == 0)
+                    return launch_swept_group<P, T, 2, PATH_SPAN4>(p, mode, phase, st, sl, nx, W, threads, s);
+            }
             return launch_swept_path<P, T, PATH_SPAN4>(p, mode, phase, st, sl, nx, W, threads, s);
         }
         constexpr int kMaxThreads = (P == SW_KS) ? 1024 : 512;

@@ -9,6 +9,7 @@
 
 #include <cuda_runtime.h>
 
+#include "exact_int.h"
 #include "sw_internal.h"
 
 // k_ks_div.cu compiles the kernel headers (this file, engine.cuh,
@@ -46,6 +47,14 @@ __device__ __forceinline__ float ab(float a) { return fabsf(a); }
 __device__ __forceinline__ double fm(double a, double b, double c) { return __fma_rn(a, b, c); }
 __device__ __forceinline__ float fm(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 
+// Products whose FP64 form runs on the integer pipe (exact_int.h), with the
+// bits of the FP64 multiply: 6 * c, and x * f with f = 2^k.  FP32 keeps its
+// multiply: the FP32 kernels are bound by instruction issue, not by a pipe.
+__device__ __forceinline__ double ml6(double c) { return mul6(c); }
+__device__ __forceinline__ float ml6(float c) { return ml(6.0f, c); }
+__device__ __forceinline__ double mlp2(double x, double f, int k) { return mul_pow2(x, f, k); }
+__device__ __forceinline__ float mlp2(float x, float f, int) { return ml(x, f); }
+
 // ---------------------------------------------------------------- Heat
 // execFunc, Heat1D_SweptShared.cu:121-130: fourier*(T[l] + T[r]) + fourierTwo*T[c]
 template <typename T>
@@ -65,15 +74,18 @@ __device__ __forceinline__ T heat_step(const Params<T> &p, T l, T c, T r) {
 // (barring overflow or underflow of the scaled terms, ~1e+-300).
 // KS_DIVIDE is the DIVISE build (KS1D_SweptShared.cu:111-132): each term divided
 // by 4dx, dx^2, dx^4, summed in the same order.
+// In FP64 two of the products run on the integer pipe with the same bits: 6c
+// (ml6) and, under KS_POW2, sec * d2 (mlp2, d2 = 2^d2_e): 12 FP64-pipe
+// operations per sub-step where the cell's square is supplied.
 template <typename T>
 __device__ __forceinline__ T ks_rhs_sq(const Params<T> &p, T ll, T l, T c, T r, T rr, T l2, T r2) {
     const T conv = sb(r2, l2);  // l2 = l*l, r2 = r*r
     const T sec = fm(T(-2), c, ad(l, r));                        // (l + r) - 2c
-    const T fourth = ad(fm(T(-4), r, ad(fm(T(-4), l, ll), ml(T(6), c))), rr);  // ((ll - 4l) + 6c) - 4r + rr
+    const T fourth = ad(fm(T(-4), r, ad(fm(T(-4), l, ll), ml6(c))), rr);  // ((ll - 4l) + 6c) - 4r + rr
 #ifdef SW_KS_DIVIDE_TU
     return ad(ad(dv(conv, p.c4), dv(sec, p.d2)), dv(fourth, p.d4));
 #else
-    if (p.ks_form == KS_POW2) return fm(fourth, p.d4, fm(conv, p.c4, ml(sec, p.d2)));
+    if (p.ks_form == KS_POW2) return fm(fourth, p.d4, fm(conv, p.c4, mlp2(sec, p.d2, p.d2_e)));
     return ad(ad(ml(conv, p.c4), ml(sec, p.d2)), ml(fourth, p.d4));
 #endif
 }
@@ -135,19 +147,21 @@ template <typename T>
 __device__ __forceinline__ Q3<T> qscale(T s, Q3<T> a) { return q3(ml(s, a.x), ml(s, a.y), ml(s, a.z)); }
 
 // pressure, Euler1D_SweptShared.cu:183-193: mgam*(E - (0.5*m*m/rho))
+// (The products by 0.5 and 2 below are exact scalings: mlp2 forms them on the
+// integer pipe in FP64, with the multiply's bits.)
 template <typename T>
 __device__ __forceinline__ T eu_pressure(const Params<T> &p, Q3<T> q) {
-    return ml(p.mgam, sb(q.z, dv(ml(ml(T(0.5), q.y), q.y), q.x)));
+    return ml(p.mgam, sb(q.z, dv(ml(mlp2(q.y, T(0.5), -1), q.y), q.x)));
 }
 // pressureHalf, :202-212: mgam*(z - 0.5*y*y)
 template <typename T>
 __device__ __forceinline__ T eu_pressure_half(const Params<T> &p, Q3<T> q) {
-    return ml(p.mgam, sb(q.z, ml(ml(T(0.5), q.y), q.y)));
+    return ml(p.mgam, sb(q.z, ml(mlp2(q.y, T(0.5), -1), q.y)));
 }
 // limitor, :222-228: cur + 0.5*min(ratio,1)*(oth - cur)
 template <typename T>
 __device__ __forceinline__ Q3<T> eu_limit(Q3<T> cur, Q3<T> oth, T ratio) {
-    return qadd(cur, qscale(ml(T(0.5), mn(ratio, T(1))), qsub(oth, cur)));
+    return qadd(cur, qscale(mlp2(mn(ratio, T(1)), T(0.5), -1), qsub(oth, cur)));
 }
 // eulerFlux, :237-257
 template <typename T>
@@ -180,13 +194,13 @@ template <typename T>
 __device__ __forceinline__ Q3<T> eu_flux_sum(const Params<T> &p, const Q3<T> (&s)[5], bool fl, bool fr) {
     const T Z = T(0);
     // Written as in the reference: P1-P0 = 2*s1.x*s0.x*(s1.z - s0.z) + (s0.y*s0.y*s1.x - s1.y*s1.y*s0.x)
-    T pLL = fl ? Z : ad(ml(ml(ml(T(2), s[1].x), s[0].x), sb(s[1].z, s[0].z)),
+    T pLL = fl ? Z : ad(ml(ml(mlp2(s[1].x, T(2), 1), s[0].x), sb(s[1].z, s[0].z)),
                         sb(ml(ml(s[0].y, s[0].y), s[1].x), ml(ml(s[1].y, s[1].y), s[0].x)));
-    T pL = ad(ml(ml(ml(T(2), s[2].x), s[1].x), sb(s[2].z, s[1].z)),
+    T pL = ad(ml(ml(mlp2(s[2].x, T(2), 1), s[1].x), sb(s[2].z, s[1].z)),
               sb(ml(ml(s[1].y, s[1].y), s[2].x), ml(ml(s[2].y, s[2].y), s[1].x)));
-    T pR = ad(ml(ml(ml(T(2), s[2].x), s[3].x), sb(s[3].z, s[2].z)),
+    T pR = ad(ml(ml(mlp2(s[2].x, T(2), 1), s[3].x), sb(s[3].z, s[2].z)),
               sb(ml(ml(s[2].y, s[2].y), s[3].x), ml(ml(s[3].y, s[3].y), s[2].x)));
-    T pRR = fr ? Z : ad(ml(ml(ml(T(2), s[3].x), s[4].x), sb(s[4].z, s[3].z)),
+    T pRR = fr ? Z : ad(ml(ml(mlp2(s[3].x, T(2), 1), s[4].x), sb(s[4].z, s[3].z)),
                         sb(ml(ml(s[3].y, s[3].y), s[4].x), ml(ml(s[4].y, s[4].y), s[3].x)));
 
     const bool skipL = (pLL == Z) || (pL == Z) || ((pLL < Z) != (pL < Z));
@@ -218,7 +232,7 @@ __device__ __forceinline__ Q3<T> eu_flux_sum(const Params<T> &p, const Q3<T> (&s
 //    the reference's order.
 template <typename T>
 __device__ __forceinline__ T eu_pdiff(Q3<T> a, Q3<T> b) {
-    return ad(ml(ml(ml(T(2), b.x), a.x), sb(b.z, a.z)), sb(ml(ml(a.y, a.y), b.x), ml(ml(b.y, b.y), a.x)));
+    return ad(ml(ml(mlp2(b.x, T(2), 1), a.x), sb(b.z, a.z)), sb(ml(ml(a.y, a.y), b.x), ml(ml(b.y, b.y), a.x)));
 }
 template <typename T>
 __device__ __forceinline__ void eu_iface(const Params<T> &p, Q3<T> am, Q3<T> a, Q3<T> b, Q3<T> bp, T Da, T Db, T Dbp,

@@ -31,8 +31,17 @@ EXPORTED = ["sw_abi_version", "sw_strerror", "sw_ctx_create", "sw_ctx_destroy", 
             "sw_run_device", "sw_plan", "sw_cli_main", "sw_run_batch", "sw_run_batch_device",
             "sw_query_tuning", "sw_run_device_noalloc", "sw_closure_infer", "sw_closure_step",
             "sw_closure_grad", "sw_closure_adam", "sw_closure_train", "sw_coarse_grain", "sw_wait_probe",
-            "sw_fp64_rates"]
+            "sw_fp64_rates", "sw_swept_pass"]
 CLOSURE_PARAMS = 5506
+CUDA_STREAM_LEGACY = 1  # cudaStreamLegacy: the legacy default stream (a stream argument of 0 means the context's own)
+
+
+def torch_stream() -> int:
+    """The handle of torch's current CUDA stream as the C ABI takes it: torch's
+    default stream is the legacy default stream, handle 0, which the ABI reads
+    as "the context's stream"; cudaStreamLegacy names it instead."""
+    import torch
+    return torch.cuda.current_stream().cuda_stream or CUDA_STREAM_LEGACY
 NOALLOC_SCRATCH_BYTES = 24 * 1024 * 1024
 
 
@@ -138,11 +147,12 @@ def library():
     L.sw_wait_probe.argtypes = [vp, C.c_int64, C.POINTER(C.c_double)]
     dp = C.POINTER(C.c_double)
     L.sw_fp64_rates.argtypes = [vp, dp, dp, dp]
+    L.sw_swept_pass.argtypes = [vp, cp, C.c_int32, C.c_int32, vp, vp, vp]
     for name in ("sw_ctx_create", "sw_ctx_destroy", "sw_config_init", "sw_validate", "sw_constants_of",
                  "sw_initial_condition", "sw_run", "sw_run_device", "sw_cli_main", "sw_plan", "sw_run_batch",
                  "sw_run_batch_device", "sw_query_tuning", "sw_run_device_noalloc", "sw_closure_infer",
                  "sw_closure_step", "sw_closure_grad", "sw_closure_adam", "sw_closure_train", "sw_coarse_grain",
-                 "sw_fp64_rates"):
+                 "sw_fp64_rates", "sw_swept_pass"):
         getattr(L, name).restype = C.c_int
     _lib = L
     return L
@@ -248,6 +258,14 @@ class Solver:
         if rc:
             raise self._err(rc, "sw_run")
         return final, res, snaps
+
+    def swept_pass(self, cfg: Config, mode: int, phase: int, state_ptr: int, slots_ptr: int, stream: int = 0) -> None:
+        """sw_swept_pass: one up (0) / diamond (1) / down (2) launch over the
+        domain's tiles on device state and slots (2 * nx cells); enqueued, not waited for."""
+        rc = self._lib.sw_swept_pass(self._ctx, C.byref(cfg), int(mode), int(phase), C.c_void_p(state_ptr),
+                                     C.c_void_p(slots_ptr), C.c_void_p(stream) if stream else None)
+        if rc:
+            raise self._err(rc, "sw_swept_pass")
 
     def run_device(self, cfg: Config, state_ptr: int, stream: int = 0) -> Result:
         """Device-resident run (sw_run_device) on a device pointer in device layout

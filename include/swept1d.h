@@ -172,6 +172,28 @@ int sw_run(sw_ctx *ctx, const sw_config *cfg, const void *ic_host, void *final_h
  * snapshots; returns when the run has completed. */
 int sw_run_device(sw_ctx *ctx, const sw_config *cfg, void *state_dev, void *stream, sw_result *out);
 
+/* One pass of the swept decomposition (the reference's upTriangle,
+ * wholeDiamond / splitDiamond or downTriangle launch; Heat1D_SweptShared.cu:
+ * 147-408, KS1D_SweptShared.cu:209-394, Euler1D_SweptShared.cu:437-746) over
+ * all tiles of the domain, enqueued on `stream` (NULL = the context's), not
+ * waited for.  cfg->alg must be SW_ALG_SWEPT; the tile width is cfg->tpb,
+ * the threads per tile cfg->threads.  mode 0 = up-triangle (phase must be
+ * 0): state -> slots; 1 = diamond: slots -> slots; 2 = down-triangle: slots
+ * -> state.  Phase 0 tiles start at t*tpb, phase 1 tiles at t*tpb + tpb/2
+ * (mod nx); diamonds alternate phases 1, 0, 1, ... after the up-triangle.
+ *
+ * slots_dev holds 2*nx cells (device layout) of edge slots, one of tpb cells
+ * per half-tile: half-tile h (cells [h*tpb/2, (h+1)*tpb/2)) owns slot cells
+ * [h*tpb, (h+1)*tpb).  A phase-1 pass reads and writes slot 0 only through
+ * the last tile, the one whose cells wrap from nx-1 to 0, and in the
+ * down-triangle that tile writes state cells [0, tpb/2).  A periodic domain
+ * split into parts that run their passes as periodic domains of their own
+ * therefore needs only that slot (before and after each phase-1 pass) and
+ * those cells (after a phase-1 down-triangle) moved between neighbours; the
+ * package's split.py does this across devices or processes. */
+int sw_swept_pass(sw_ctx *ctx, const sw_config *cfg, int32_t mode, int32_t phase, void *state_dev, void *slots_dev,
+                  void *stream);
+
 /* What a run would do, without a device: the time bookkeeping of
  * classicWrapper / sweptWrapper (Heat1D_SweptShared.cu:483-510,541-682;
  * KS1D_SweptShared.cu:609-631,676-851; Euler1D_SweptShared.cu:855-888,924-1100).
