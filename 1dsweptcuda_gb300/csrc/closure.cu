@@ -47,9 +47,26 @@ constexpr int THREADS = 256;
 constexpr int OW1 = 0, OB1 = 160, OW2 = 192, OB2 = 5312, OW3 = 5344, OB3 = 5504, OSCALE = 5505;
 constexpr int NTRAIN = 5505, NPARAM = 5506;
 
-__device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f)); }
+// GELU in its tanh form (Hendrycks & Gimpel, "Gaussian Error Linear Units",
+// 2016): gelu(x) = x/2 (1 + tanh(c (x + a x^3))), c = sqrt(2/pi), a = 0.044715,
+// with tanh from the SFU's tanh.approx.f32 (relative error below 2^-10.7):
+// a handful of instructions where the erf form took a long polynomial, and
+// the step is bound by instruction issue.  oracle/closure.py restates the same
+// function (with an exact tanh).
+constexpr float kGeluC = 0.79788456080286536f, kGeluA = 0.044715f;
+__device__ __forceinline__ float tanh_sfu(float x) {
+    float y;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float gelu(float x) {
+    const float t = tanh_sfu(kGeluC * x * fmaf(kGeluA * x, x, 1.0f));
+    return 0.5f * x * (1.0f + t);
+}
 __device__ __forceinline__ float gelu_grad(float x) {
-    return 0.5f * (1.0f + erff(x * 0.70710678118654752f)) + x * 0.39894228040143268f * expf(-0.5f * x * x);
+    const float x2 = x * x;
+    const float t = tanh_sfu(kGeluC * x * fmaf(kGeluA, x2, 1.0f));
+    return fmaf(0.5f * x * (1.0f - t * t), kGeluC * fmaf(3.0f * kGeluA, x2, 1.0f), 0.5f * (1.0f + t));
 }
 __device__ __forceinline__ float bf16r(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
 __device__ __forceinline__ uint32_t pack2(__nv_bfloat16 lo, __nv_bfloat16 hi) {
@@ -74,8 +91,9 @@ struct Smem {
     float w1[CH * KW], b1[CH], b2[CH], w3[CH * KW], b3, scale;
     __nv_bfloat16 a1[NA1 * LDB];                   // layer-1 activations, BF16 (the MMA A operand)
     alignas(16) __nv_bfloat16 w2[KW * CH * LDB];   // w2[t][o][i], i contiguous (the MMA B operand)
-    float a2[NA2 * LDF];                           // layer-2 activations gelu(z2)
     float pred[TOUT + 4];                          // k_step: the KS predictor on x0-2 .. x0+TOUT+1
+    float p3[KW * NA2];                            // forward: p3[t][r] = sum_i w3[i][t] a2[r][i]
+    float a2[NA2 * LDF];                           // layer-2 activations gelu(z2) (backward only)
     float z2[NA2 * LDF];                           // layer-2 pre-activations (backward only)
     float z1[NA1 * LDF];                           // layer-1 pre-activations (backward only)
 };
@@ -127,8 +145,13 @@ __device__ void load_tile(Smem &s, const float *__restrict__ theta, const float 
     }
 }
 
-// Layers 1 and 2 of the forward pass: a1 (BF16) and a2 = gelu(z2) (FP32); with
-// TRAIN also the pre-activations z1 and z2.  Requires load_tile and a barrier first.
+// Layers 1 and 2 of the forward pass.  TRAIN: a1 (BF16), a2 = gelu(z2) (FP32)
+// and the pre-activations z1, z2 for the backward pass.  Otherwise layer 3's
+// per-row tap sums p3[t][r] = sum_i w3[i][t] gelu(z2[r][i]) are formed in the
+// MMA epilogue, so a2 is never stored: each lane holds 8 channels of rows r
+// and r + 8, dots them with w3 for the five taps, and the four lanes of a row
+// add their sums by shuffles (output q is then b3 + sum_t p3[t][q + t]).
+// Requires load_tile and a barrier first.
 template <bool TRAIN>
 __device__ void forward_12(Smem &s) {
     {
@@ -179,34 +202,66 @@ __device__ void forward_12(Smem &s) {
                 }
             }
         }
+        const int r0 = p0 + g, r1 = p0 + g + 8;
+        if constexpr (TRAIN) {
 #pragma unroll
-        for (int nt = 0; nt < 4; ++nt) {
-            const int o = nt * 8 + 2 * q;
-            const int r0 = p0 + g, r1 = p0 + g + 8;
-            if (r0 < NA2) {
-                const float z0 = acc[nt][0] + s.b2[o], z1 = acc[nt][1] + s.b2[o + 1];
-                if (TRAIN) {
+            for (int nt = 0; nt < 4; ++nt) {
+                const int o = nt * 8 + 2 * q;
+                if (r0 < NA2) {
+                    const float z0 = acc[nt][0] + s.b2[o], z1 = acc[nt][1] + s.b2[o + 1];
                     s.z2[r0 * LDF + o] = z0;
                     s.z2[r0 * LDF + o + 1] = z1;
+                    s.a2[r0 * LDF + o] = gelu(z0);
+                    s.a2[r0 * LDF + o + 1] = gelu(z1);
                 }
-                s.a2[r0 * LDF + o] = gelu(z0);
-                s.a2[r0 * LDF + o + 1] = gelu(z1);
-            }
-            if (r1 < NA2) {
-                const float z2 = acc[nt][2] + s.b2[o], z3 = acc[nt][3] + s.b2[o + 1];
-                if (TRAIN) {
+                if (r1 < NA2) {
+                    const float z2 = acc[nt][2] + s.b2[o], z3 = acc[nt][3] + s.b2[o + 1];
                     s.z2[r1 * LDF + o] = z2;
                     s.z2[r1 * LDF + o + 1] = z3;
+                    s.a2[r1 * LDF + o] = gelu(z2);
+                    s.a2[r1 * LDF + o + 1] = gelu(z3);
                 }
-                s.a2[r1 * LDF + o] = gelu(z2);
-                s.a2[r1 * LDF + o + 1] = gelu(z3);
+            }
+        } else {
+            float p[2][KW] = {};
+#pragma unroll
+            for (int nt = 0; nt < 4; ++nt) {
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    const int o = nt * 8 + 2 * q + (e & 1);
+                    const float a = gelu(acc[nt][e] + s.b2[o]);
+#pragma unroll
+                    for (int t = 0; t < KW; ++t) p[e >> 1][t] = fmaf(s.w3[o * KW + t], a, p[e >> 1][t]);
+                }
+            }
+#pragma unroll
+            for (int h = 0; h < 2; ++h)
+#pragma unroll
+                for (int t = 0; t < KW; ++t) {
+                    p[h][t] += __shfl_xor_sync(0xffffffffu, p[h][t], 1);
+                    p[h][t] += __shfl_xor_sync(0xffffffffu, p[h][t], 2);
+                }
+            if (q == 0) {
+#pragma unroll
+                for (int t = 0; t < KW; ++t) {
+                    if (r0 < NA2) s.p3[t * NA2 + r0] = p[0][t];
+                    if (r1 < NA2) s.p3[t * NA2 + r1] = p[1][t];
+                }
             }
         }
     }
     __syncthreads();
 }
 
-// Layer 3 for output q: b3 + sum_{t,i} w3[i][t] * a2[q + t][i].
+// Layer 3 for output q from the epilogue's tap sums: b3 + sum_t p3[t][q + t].
+__device__ __forceinline__ float layer3_sums(const Smem &s, int q) {
+    float d = 0.0f;
+#pragma unroll
+    for (int t = 0; t < KW; ++t) d += s.p3[t * NA2 + q + t];
+    return d + s.b3;
+}
+
+// Layer 3 for output q (backward pass, from the stored a2): b3 + sum_{t,i} w3[i][t] * a2[q + t][i].
 __device__ __forceinline__ float layer3(const Smem &s, int q) {
     float d = 0.0f;
 #pragma unroll
@@ -228,7 +283,7 @@ __global__ void __launch_bounds__(THREADS) k_infer(const float *__restrict__ the
     load_tile(s, theta, ud, n, x0, w2p);
     __syncthreads();
     forward_12<false>(s);
-    for (int q = threadIdx.x; q < TOUT; q += blockDim.x) delta[dom * n + x0 + q] = s.scale * layer3(s, q);
+    for (int q = threadIdx.x; q < TOUT; q += blockDim.x) delta[dom * n + x0 + q] = s.scale * layer3_sums(s, q);
 }
 
 // One coarse KS step fused with the closure: u_out = classic KS step(u_in) + f(u_in).
@@ -252,7 +307,7 @@ __global__ void __launch_bounds__(THREADS) k_step(const float *__restrict__ thet
     for (int q = threadIdx.x; q < TOUT; q += blockDim.x) {
         const int c = q + 6, j = q + 2;  // us index of x0+q; predictor index of x0+q
         float v = ks_correct(pk, s.us[c], s.pred[j - 2], s.pred[j - 1], s.pred[j], s.pred[j + 1], s.pred[j + 2]);
-        if (use_closure) v += s.scale * layer3(s, q);
+        if (use_closure) v += s.scale * layer3_sums(s, q);
         out[dom * n + x0 + q] = v;
     }
 }
@@ -450,7 +505,7 @@ __global__ void k_coarse_grain(const double *__restrict__ fine, float *__restric
 }
 
 constexpr size_t smem_bytes() { return sizeof(Smem); }
-constexpr size_t smem_fwd_bytes() { return offsetof(Smem, z2); }
+constexpr size_t smem_fwd_bytes() { return offsetof(Smem, a2); }
 
 }  // namespace cl
 }  // namespace sw

@@ -108,10 +108,10 @@ __device__ __forceinline__ Ends tile_ends(int64_t base, int64_t nx, int W, int R
 }
 
 // One Heat / KS sub-step of parity `par` (1: predictor / odd Heat step; 0:
-// corrector / even Heat step) at tile cell x.  (Euler levels run euler_level.)
+// corrector / even Heat step) at tile cell x.  (Euler levels run euler_level_tile.)
 template <int P, typename T>
 __device__ __forceinline__ void tile_point(const Params<T> &p, T *rows, int L, int par, int x, Ends e) {
-    static_assert(P != SW_EULER, "Euler tile levels share interfaces across a warp (euler_level)");
+    static_assert(P != SW_EULER, "Euler tile levels compute each interface once (euler_level_tile)");
     constexpr int R = Scheme<P, T>::R;
     const T *src = rows + (par ^ 1) * L + R;
     T *dst = rows + par * L + R;
@@ -303,50 +303,17 @@ __device__ __forceinline__ void tile_span4(const Params<T> &p, T *rows, int L, i
         if (x0 + i >= lo && x0 + i < hi) dst[x0 + i] = o[i];
 }
 
-// Euler sub-step over tile cells [lo, hi) with every interface computed once.
-// A warp takes 29 cells at a time: lane l (cell b = s0 + l) loads cells
-// b-2..b+1, forms D(b-2, b-1) and the interface (b-1, b) -- taking D(b-1, b)
-// and D(b, b+1) from lanes l+1 and l+2 -- and adds its own interface minus the
-// one of lane l+1.  Lanes 29..31 only feed lanes below them; loop bounds are
-// warp-uniform so that every lane reaches every shuffle.  Values read past
-// W + R - 1 (clamped) only reach lanes whose cells are not stored.
+// The classic Euler kernel's warp scheme (k_classic_euler): a warp takes 29
+// cells at a time; lane l (cell b = s0 + l) loads cells b-2..b+1, forms
+// D(b-2, b-1) and the interface (b-1, b) -- taking D(b-1, b) and D(b, b+1)
+// from lanes l+1 and l+2 -- and adds its own interface minus the one of lane
+// l+1.  Lanes 29..31 only feed lanes below them.
 constexpr int kEulerCellsPerWarp = 29;
 
 template <typename T>
 __device__ __forceinline__ Q3<T> shfl_down3(Q3<T> v, int d) {
     return q3(__shfl_down_sync(0xffffffffu, v.x, d), __shfl_down_sync(0xffffffffu, v.y, d),
               __shfl_down_sync(0xffffffffu, v.z, d));
-}
-
-template <typename T>
-__device__ __forceinline__ void euler_level(const Params<T> &p, T *rows, int L, int W, int par, int lo, int hi, Ends e) {
-    constexpr int R = Scheme<SW_EULER, T>::R;
-    const T *src = rows + (par ^ 1) * 3 * L + R;
-    T *dst = rows + par * 3 * L + R;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-    const T scale = par ? ml(T(0.25), p.dtdx) : ml(T(0.5), p.dtdx);
-    for (int s0 = lo + warp * kEulerCellsPerWarp; s0 < hi; s0 += nwarp * kEulerCellsPerWarp) {
-        const int b = s0 + lane;
-        Q3<T> c[4];
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const int x = min(b - 2 + k, W + R - 1);
-            c[k] = q3(src[x], src[L + x], src[2 * L + x]);
-        }
-        // zero across the domain's ends (the reference's edge flags, Euler1D_SweptShared.cu:311-335)
-        const T D = (b - 1 == e.first || b - 2 == e.last) ? T(0) : eu_pdiff(c[0], c[1]);
-        const T D1 = __shfl_down_sync(0xffffffffu, D, 1), D2 = __shfl_down_sync(0xffffffffu, D, 2);
-        Q3<T> F, S;
-        eu_iface(p, c[0], c[1], c[2], c[3], D, D1, D2, F, S);
-        const Q3<T> Fr = shfl_down3(F, 1), Sr = shfl_down3(S, 1);
-        if (lane < kEulerCellsPerWarp && b < hi && b != e.first && b != e.last) {
-            const Q3<T> base = par ? c[2] : q3(dst[b], dst[L + b], dst[2 * L + b]);
-            const Q3<T> o = qadd(base, qscale(scale, eu_combine(F, S, Fr, Sr)));
-            dst[b] = o.x;
-            dst[L + b] = o.y;
-            dst[2 * L + b] = o.z;
-        }
-    }
 }
 
 // Euler sub-step over tile cells [lo, hi) of a swept tile, every interface
@@ -358,11 +325,12 @@ __device__ __forceinline__ void euler_level(const Params<T> &p, T *rows, int L, 
 //   B. the flux F_b and dissipation S_b of each interface (b-1, b), b in
 //      [lo, hi+1), from the four cells around it and D_{b-1}, D_b, D_{b+1};
 //   C. each cell's update from its two interfaces (eu_combine).
-// Same operations on the same values as euler_level (and so as the
-// reference's per-cell form), but every lane of pass B computes an interface
-// that is used: euler_level's 29-cell warps spend 3 lanes of 32 on terms only
-// their neighbours need.  The cells read lie in [lo-2, hi+1], inside the row
-// and its margins, as for euler_level.
+// Same operations on the same values as the classic kernel's warp scheme
+// (and so as the reference's per-cell form), but every lane of pass B
+// computes an interface that is used, where 29-cell warps spend 3 lanes of 32
+// on terms only their neighbours need.  The cells read lie in [lo-2, hi+1],
+// inside the row and its margins: the down part's widest level reads row 1's
+// imported cells -2 .. W+1.
 template <typename T>
 __device__ __forceinline__ void euler_level_tile(const Params<T> &p, T *rows, int L, int par, int lo, int hi, Ends e) {
     constexpr int R = Scheme<SW_EULER, T>::R;
@@ -407,7 +375,7 @@ __device__ __forceinline__ void euler_level_tile(const Params<T> &p, T *rows, in
 // Which cell mapping a kernel carries: PATH_ANY picks at run time (blockDim.x
 // * 4 == W: 4 cells per thread), PATH_CELL and PATH_SPAN4 hold only one, so a
 // kernel does not pay the registers of a path it never runs.  Euler always
-// runs euler_level.
+// runs euler_level_tile.
 enum TilePath { PATH_ANY = 0, PATH_CELL = 1, PATH_SPAN4 = 2 };
 
 // Heat / KS cells [lo, hi) of one level, one per thread from the lowest thread,
@@ -548,7 +516,7 @@ __device__ __forceinline__ void swept_tile(const Params<T> &p, typename Scheme<P
 // Euler level is three passes with a barrier after each, and other blocks'
 // warps keep the FP64 pipe busy through them.
 #ifndef SW_EULER_MIN_BLOCKS
-#define SW_EULER_MIN_BLOCKS 4
+#define SW_EULER_MIN_BLOCKS 3
 #endif
 template <int P, typename T, int PATH>
 constexpr int swept_min_blocks() {
@@ -628,8 +596,8 @@ __global__ void __launch_bounds__(Scheme<P, T>::CMAXT) k_classic(const Params<T>
     if (g < p.nx) classic_cell<P, T>(p, in, out, sub, g);
 }
 
-// Classic Euler sub-step with shared interfaces (the warp scheme of
-// euler_level over the whole domain, 29 cells per warp).  Cells 0 and nx-1
+// Classic Euler sub-step with shared interfaces (the warp scheme above over
+// the whole domain, 29 cells per warp).  Cells 0 and nx-1
 // hold the Dirichlet states (classicEuler, Euler1D_SweptShared.cu:400-426).
 template <typename T>
 __global__ void __launch_bounds__(256) k_classic_euler(const Params<T> p, const V4<T> *__restrict__ in,
@@ -700,26 +668,12 @@ __device__ __forceinline__ int group_slot(int t, int n) {
     for (int q = 1; q < G; ++q) k += (t >= q * n) ? 1 : 0;
     return k;
 }
-// SW_GROUP_ROTATE: a level's packed cells start at warp `rot` (mod the
-// block's warps) instead of warp 0, rot = (level + block) mod 4.  A warp's SM
-// sub-partition is its index mod 4, so a level's last, part-filled warp then
-// lands on a different sub-partition from level to level and from block to
-// block, instead of always on the first.
-#ifndef SW_GROUP_ROTATE
-#define SW_GROUP_ROTATE 0
-#endif
 template <int P, typename T, int G, int PATH>
 __device__ __forceinline__ void group_level(const Params<T> &p, T *rows, int TS, int L, int par, int lo, int hi,
-                                            const Ends (&e)[G], int level) {
+                                            const Ends (&e)[G]) {
     // threads per tile at this level
     const int n = (PATH == PATH_SPAN4) ? ((hi - (lo & ~3) + 3) >> 2) : (hi - lo);
-#if SW_GROUP_ROTATE
-    int t = (int)threadIdx.x - 32 * ((level + (int)blockIdx.x) & 3);
-    if (t < 0) t += (int)blockDim.x;
-#else
     const int t = (int)threadIdx.x;
-    (void)level;
-#endif
     if (t < G * n) {
         const int k = group_slot<G>(t, n);
         Ends ek = e[0];
@@ -734,7 +688,7 @@ __device__ __forceinline__ void group_level(const Params<T> &p, T *rows, int TS,
 template <int P, typename T, int MODE, int G, int PATH>
 __device__ __forceinline__ void swept_tile_group(const Params<T> &p, T *__restrict__ state, T *__restrict__ slots,
                                                  T *rows, const int W, const int phase, const int64_t t0) {
-    static_assert(P != SW_EULER, "Euler levels run euler_level");
+    static_assert(P != SW_EULER, "Euler levels run euler_level_tile");
     constexpr int R = Scheme<P, T>::R;
     const int L = row_stride(W), h = W >> 1, H = W / (2 * R), TS = tile_rows<P>() * L;
     const int64_t nx = p.nx, nhalf = nx / h;
@@ -756,9 +710,9 @@ __device__ __forceinline__ void swept_tile_group(const Params<T> &p, T *__restri
     __syncthreads();
     if constexpr (MODE != MODE_UP) {  // down part, two levels per iteration (H is even)
         for (int j = 1; j < H; j += 2) {
-            group_level<P, T, G, PATH>(p, rows, TS, L, 1, h - j * R, h + j * R, e, j);
+            group_level<P, T, G, PATH>(p, rows, TS, L, 1, h - j * R, h + j * R, e);
             __syncthreads();
-            group_level<P, T, G, PATH>(p, rows, TS, L, 0, h - (j + 1) * R, h + (j + 1) * R, e, j + 1);
+            group_level<P, T, G, PATH>(p, rows, TS, L, 0, h - (j + 1) * R, h + (j + 1) * R, e);
             __syncthreads();
         }
     }
@@ -770,12 +724,12 @@ __device__ __forceinline__ void swept_tile_group(const Params<T> &p, T *__restri
     } else {
         int u = 1;
         for (; u + 1 < H; u += 2) {
-            group_level<P, T, G, PATH>(p, rows, TS, L, 1, u * R, W - u * R, e, u);
+            group_level<P, T, G, PATH>(p, rows, TS, L, 1, u * R, W - u * R, e);
             __syncthreads();
-            group_level<P, T, G, PATH>(p, rows, TS, L, 0, (u + 1) * R, W - (u + 1) * R, e, u + 1);
+            group_level<P, T, G, PATH>(p, rows, TS, L, 0, (u + 1) * R, W - (u + 1) * R, e);
             __syncthreads();
         }
-        group_level<P, T, G, PATH>(p, rows, TS, L, 1, u * R, W - u * R, e, u);  // u = H - 1
+        group_level<P, T, G, PATH>(p, rows, TS, L, 1, u * R, W - u * R, e);  // u = H - 1
         __syncthreads();
         for (int i = threadIdx.x; i < G * W; i += blockDim.x) {
             const int k = i / W, x = i - k * W;

@@ -2,7 +2,7 @@
 
 The network corrects a coarse KS step: delta = f(u), u one periodic coarse
 domain, f = conv5(32->1) . GELU . conv5(32->32) . GELU . conv5(1->32), circular
-padding 2 on every layer.  Parameters are kept in FP32 and rounded to BF16
+padding 2 on every layer, GELU in its tanh form.  Parameters are kept in FP32 and rounded to BF16
 for the forward pass; the 32->32 layer multiplies BF16 activations by BF16
 weights with FP32 accumulation (the tensor-core layer), the outer layers run
 in FP32 with the BF16-rounded weights.  This module restates that arithmetic
@@ -69,14 +69,19 @@ def init(seed: int = 0, scale: float = 1.0) -> np.ndarray:
     return pack(d).astype(np.float32)
 
 
+# GELU in its tanh form (Hendrycks & Gimpel, "Gaussian Error Linear Units",
+# 2016): x/2 (1 + tanh(c (x + a x^3))), c = sqrt(2/pi), a = 0.044715 -- the
+# form the kernels evaluate (with the SFU's tanh.approx.f32; here an exact tanh).
+GELU_C, GELU_A = math.sqrt(2.0 / math.pi), 0.044715
+
+
 def gelu(x):
-    from scipy.special import erf
-    return 0.5 * x * (1.0 + erf(x / math.sqrt(2.0)))
+    return 0.5 * x * (1.0 + np.tanh(GELU_C * (x + GELU_A * x ** 3)))
 
 
 def gelu_grad(x):
-    from scipy.special import erf
-    return 0.5 * (1.0 + erf(x / math.sqrt(2.0))) + x * np.exp(-0.5 * x * x) / math.sqrt(2.0 * math.pi)
+    t = np.tanh(GELU_C * (x + GELU_A * x ** 3))
+    return 0.5 * (1.0 + t) + 0.5 * x * (1.0 - t * t) * GELU_C * (1.0 + 3.0 * GELU_A * x * x)
 
 
 def _taps(a: np.ndarray) -> np.ndarray:
