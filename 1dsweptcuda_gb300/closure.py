@@ -198,15 +198,16 @@ def run_adaptive(solver, closure: Closure, fine0, coarse_steps: int, segment: in
     fine0: (n_dom, 4096) FP64 states at t0 (the problem as posed); the coarse
     state starts at CG(fine0).  The judge is a shadow: the fine solver
     advances the exact fine state of a seeded sample of the domains (one in
-    `shadow_every`) alongside the coarse run, on the context `judge` (its own
-    by default, so that its captured graphs stay warm).  Before the first
+    `shadow_every`) alongside the coarse run, on the context `judge` (default:
+    the run's own; a context of its own keeps its captured graphs warm).  Before the first
     segment both coarse variants advance the sample and the one nearer the
-    coarse-grained shadow (largest relative L2 error over the sample) is
+    coarse-grained shadow (mean relative L2 error over the sample) is
     picked; after that the ensemble runs each segment with the current pick
     while the other variant advances the sample alone, and the pick changes
     when the other variant ends the segment nearer the shadow -- so the
     closure is used exactly where it beats the plain step.  The sample's
-    error after each segment is the run's certificate.  When it passes tau,
+    mean relative L2 error after each segment is the run's certificate (its
+    largest error is reported beside it).  When it passes tau,
     or its growth over the last segment extrapolated linearly to the end
     passes tau, the run stops and every domain is solved by the fine solver
     from fine0 in one batch, so the answer is the fine solution itself.
@@ -237,7 +238,7 @@ def run_adaptive(solver, closure: Closure, fine0, coarse_steps: int, segment: in
                 v = sample.clone()
                 closure.step(v, k, use_closure=on[name])
                 runs[name] = err_of(v, ref)
-            pick = min(runs, key=lambda nm: float(runs[nm].max()))
+            pick = min(runs, key=lambda nm: float(runs[nm].mean()))
             closure.step(u, k, use_closure=on[pick])
             e_cur, e_alt = runs[pick], runs["plain" if pick == "closure" else "closure"]
         else:
@@ -247,17 +248,18 @@ def run_adaptive(solver, closure: Closure, fine0, coarse_steps: int, segment: in
             closure.step(u, k, use_closure=on[pick])
             e_cur, e_alt = err_of(u[idx], ref), err_of(v, ref)
         used = pick
-        err = float(e_cur.max())
+        err = float(e_cur.mean())   # the certificate: the sample's mean relative L2 error (the metric's form)
         done += k
-        info[used] += 1
-        info["log"].append({"t": done * COARSE_DT, "used": used, "err": err, "err_other": float(e_alt.max())})
-        info["shadow_max_rel_l2"], info["shadow_mean_rel_l2"] = err, float(e_cur.mean())
+        info["log"].append({"t": done * COARSE_DT, "used": used, "err": err, "err_max": float(e_cur.max()),
+                            "err_other": float(e_alt.mean())})
         left = (coarse_steps - done) / max(k, 1)   # segments still to run
         if err > tau or err + max(err - prev, 0.0) * left > tau:
             info["fallback"] = True
             break
+        info[used] += 1
+        info["shadow_mean_rel_l2"], info["shadow_max_rel_l2"] = err, float(e_cur.max())
         prev = err
-        if float(e_alt.max()) < err:
+        if float(e_alt.mean()) < err:
             pick = "plain" if used == "closure" else "closure"
     if info["fallback"]:
         f = fine0.clone()
@@ -279,17 +281,25 @@ def _timed(fn):
     return out, time.perf_counter() - a
 
 
-def train_closure(solver, n_train: int = 512, snapshots: int = 64, train_steps: int = 3000, seed: int = 0):
+def train_closure(solver, n_train: int = 512, snapshots: int = 64, train_steps: int = 3000, seed: int = 0,
+                  lr: float = 2e-3, decay: bool = False):
     """A closure trained on the fine solver's own trajectories in developed
-    chaos (t >= 250), and a summary of the training."""
-    torch = _torch()
+    chaos (t >= 250), and a summary of the training.  decay: the steps run in
+    three equal phases at lr, lr / 4 and lr / 16 (a step schedule; Adam's
+    moments restart with each phase)."""
     closure = Closure(solver, seed=seed)
-    info = {"n_train_traj": n_train, "snapshots": snapshots}
+    info = {"n_train_traj": n_train, "snapshots": snapshots, "train_steps": train_steps, "lr": lr,
+            "lr_decay": decay}
     (x, y), info["datagen_s"] = _timed(lambda: make_training_data(solver, closure, n_train, snapshots, interval=25,
                                                                   seed=seed + 1, spinup=CHAOS_SPINUP))
     info["output_scale"] = closure.calibrate(y)
-    losses, info["train_s"] = _timed(lambda: closure.train(x, y, steps=train_steps, batch=64, lr=2e-3,
-                                                           seed=seed + 2))
+    phases = [(train_steps // 3, lr), (train_steps // 3, lr / 4), (train_steps - 2 * (train_steps // 3), lr / 16)] \
+        if decay else [(train_steps, lr)]
+
+    def run():
+        return np.concatenate([closure.train(x, y, steps=n, batch=64, lr=r, seed=seed + 2 + i)
+                               for i, (n, r) in enumerate(phases)])
+    losses, info["train_s"] = _timed(run)
     info["loss_first"], info["loss_last"] = float(losses[:10].mean()), float(losses[-50:].mean())
     hx, hy = make_training_data(solver, closure, 32, 8, interval=25, seed=seed + 999, spinup=CHAOS_SPINUP)
     info["heldout_defect_ratio"] = float(((hy - closure.infer(hx)).pow(2).sum() / hy.pow(2).sum()).item())
@@ -333,6 +343,7 @@ def evaluate_regime(solver, closure: Closure, fine0, horizons, tau: float = 1e-3
         row["fallback"] = info["fallback"]
         row["segments_closure"], row["segments_plain"] = info["closure"], info["plain"]
         row["shadow_domains"] = info["shadow_domains"]
+        row["shadow_mean_rel_l2"] = info.get("shadow_mean_rel_l2")
         row["shadow_max_rel_l2"] = info.get("shadow_max_rel_l2")
         row["speedup_adaptive_vs_fine"] = t_fine / row["time_adaptive_s"]
         for name in ("plain", "closure"):
@@ -355,7 +366,7 @@ def largest_certified(rows, tau: float, min_speedup: float = 5.0) -> dict:
 
 def evaluate(n_train: int = 512, snapshots: int = 64, n_eval: int = 1024, ic_horizons=(10.0, 20.0, 30.0, 40.0),
              chaos_horizons=(0.1, 0.14, 0.18, 0.2, 0.5), train_steps: int = 6000, seed: int = 0, tau: float = 1e-3,
-             segment: int = 50, shadow_every: int = 64, solver=None) -> dict:
+             segment: int = 50, shadow_every: int = 64, solver=None, decay: bool = False) -> dict:
     """Train a closure on developed chaos, then evaluate the 1024-domain
     ensemble in two regimes: from the initial condition (t0 = 0, where the
     fields are smooth until t ~ 40) and from developed chaos (t0 = 250).
@@ -364,7 +375,7 @@ def evaluate(n_train: int = 512, snapshots: int = 64, n_eval: int = 1024, ic_hor
     sw = _sw()
     own = solver is None
     solver = solver or sw.Solver(0)
-    closure, out = train_closure(solver, n_train, snapshots, train_steps, seed)
+    closure, out = train_closure(solver, n_train, snapshots, train_steps, seed, decay=decay)
     out.update({"fine_nx": FINE_NX, "coarse_nx": COARSE_NX, "n_eval": n_eval, "tau": tau, "segment": segment,
                 "shadow_every": shadow_every})
     fine0 = fine_ensemble(n_eval, seed=seed + 5)
@@ -384,8 +395,9 @@ def evaluate(n_train: int = 512, snapshots: int = 64, n_eval: int = 1024, ic_hor
 def bench_target(solver) -> dict:
     """The surrogate-corrected ensemble's line for the benchmark: the
     1024-domain, fine 4096 / coarse 1024 configuration, closure trained here on
-    512 fine trajectories x 64 snapshots of developed chaos, tau = 1e-3."""
-    out = evaluate(n_train=512, snapshots=64, n_eval=1024, train_steps=6000, solver=solver)
+    512 fine trajectories x 64 snapshots of developed chaos (18000 Adam steps,
+    step-decayed rate), tau = 1e-3."""
+    out = evaluate(n_train=512, snapshots=64, n_eval=1024, train_steps=18000, decay=True, solver=solver)
     out["note"] = ("time-to-tf at mean rel-L2 <= 1e-3 against the coarse-grained fine FP64 solution; "
                    "tf = 200 lies beyond KS's predictability horizon for any coarse scheme (errors grow e-fold "
                    "every ~4 time units in developed chaos), so the adaptive run falls back to the fine solver there")
@@ -431,6 +443,7 @@ if __name__ == "__main__":
     ap.add_argument("--tau", type=float, default=1e-3)
     ap.add_argument("--segment", type=int, default=50)
     ap.add_argument("--shadow-every", type=int, default=64)
+    ap.add_argument("--decay", action="store_true", help="step learning-rate schedule (lr, lr/4, lr/16)")
     ap.add_argument("--json", default=None)
     ap.add_argument("--bench-step", type=int, default=0, help="only time this many fused closure steps")
     a = ap.parse_args()
@@ -439,7 +452,7 @@ if __name__ == "__main__":
         sys.exit(0)
     res = evaluate(a.train_traj, a.snapshots, a.eval, [float(t) for t in a.ic_horizons.split(",")],
                    [float(t) for t in a.chaos_horizons.split(",")], a.train_steps, tau=a.tau, segment=a.segment,
-                   shadow_every=a.shadow_every)
+                   shadow_every=a.shadow_every, decay=a.decay)
     print(json.dumps(res, indent=1))
     if a.json:
         Path(a.json).write_text(json.dumps(res, indent=1))

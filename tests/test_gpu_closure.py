@@ -156,6 +156,7 @@ def test_adaptive_judge_is_the_fine_solution_of_its_sample(sw, solver, cl):
     err = (u.double() - ref.double()).norm(dim=1) / ref.double().norm(dim=1)
     sample = cl.shadow_domains(64, 16, 0)
     assert abs(float(err[sample].max()) - info["shadow_max_rel_l2"]) < 1e-12
+    assert abs(float(err[sample].mean()) - info["shadow_mean_rel_l2"]) < 1e-12
     assert float(err.max()) < tau, err
 
 
