@@ -183,6 +183,28 @@ def rel_l2(a, b) -> float:
     return float((num / den).mean().item())
 
 
+class _Background:
+    """fn() run in a thread; result() joins it and returns (or raises) its outcome."""
+
+    def __init__(self, fn):
+        import threading
+        self._out, self._err = None, None
+
+        def body():
+            try:
+                self._out = fn()
+            except BaseException as e:  # re-raised in result()
+                self._err = e
+        self._t = threading.Thread(target=body, daemon=True)
+        self._t.start()
+
+    def result(self):
+        self._t.join()
+        if self._err is not None:
+            raise self._err
+        return self._out
+
+
 def shadow_domains(n_dom: int, every: int, seed: int = 0):
     """The judge's sample: one domain in each run of `every`, at a seeded offset."""
     torch = _torch()
@@ -199,7 +221,8 @@ def run_adaptive(solver, closure: Closure, fine0, coarse_steps: int, segment: in
     state starts at CG(fine0).  The judge is a shadow: the fine solver
     advances the exact fine state of a seeded sample of the domains (one in
     `shadow_every`) alongside the coarse run, on the context `judge` (default:
-    the run's own; a context of its own keeps its captured graphs warm).  Before the first
+    one made for the call; pass one to keep its captured graphs warm across
+    calls), in a thread, so that it overlaps the coarse runs.  Before the first
     segment both coarse variants advance the sample and the one nearer the
     coarse-grained shadow (mean relative L2 error over the sample) is
     picked; after that the ensemble runs each segment with the current pick
@@ -215,11 +238,21 @@ def run_adaptive(solver, closure: Closure, fine0, coarse_steps: int, segment: in
     Returns (u, info): u (n_dom, 1024) FP32 at t0 + coarse_steps * 0.02, and
     the segments run with the closure and plain, whether it fell back, the
     sample's final error (max and mean) and a per-segment log."""
-    judge = judge or solver
+    torch = _torch()
+    own_judge = judge is None or judge is solver   # a context serves one host thread at a time
+    if own_judge:
+        judge = _sw().Solver(solver.device)
     u = coarse_grain(solver, fine0)
     n_dom = u.shape[0]
     idx = shadow_domains(n_dom, shadow_every, seed)
-    shadow = fine0[idx].contiguous().clone()
+    # the shadow lives in a buffer kept with the judge: the fine solver's captured graph is
+    # tied to its state's address, so the same buffer lets later calls replay that graph
+    shadow = getattr(judge, "_shadow_buf", None)
+    if shadow is None or shadow.shape != (int(idx.numel()), fine0.shape[1]):
+        shadow = torch.empty((int(idx.numel()), fine0.shape[1]), dtype=fine0.dtype, device=fine0.device)
+        judge._shadow_buf = shadow
+    shadow.copy_(fine0[idx])
+    torch.cuda.synchronize()   # the shadow is read on the judge's stream from here on
     info = {"closure": 0, "plain": 0, "fallback": False, "shadow_domains": int(idx.numel()), "log": []}
     on = {"plain": False, "closure": True}
 
@@ -230,22 +263,26 @@ def run_adaptive(solver, closure: Closure, fine0, coarse_steps: int, segment: in
     while done < coarse_steps:
         k = min(segment, coarse_steps - done)
         sample = u[idx].contiguous()
-        advance_fine(judge, shadow, k * FACTOR)
-        ref = coarse_grain(judge, shadow)
+        # the judge's fine segment runs on its own context and stream, in a thread (the
+        # library releases the interpreter while it waits), overlapping the coarse runs
+        judged = _Background(lambda: (advance_fine(judge, shadow, k * FACTOR), coarse_grain(judge, shadow))[1])
         if pick is None:  # first segment: both variants on the sample, then the ensemble with the better one
             runs = {}
             for name in on:
                 v = sample.clone()
                 closure.step(v, k, use_closure=on[name])
-                runs[name] = err_of(v, ref)
-            pick = min(runs, key=lambda nm: float(runs[nm].mean()))
+                runs[name] = v
+            ref = judged.result()
+            errs = {name: err_of(v, ref) for name, v in runs.items()}
+            pick = min(errs, key=lambda nm: float(errs[nm].mean()))
             closure.step(u, k, use_closure=on[pick])
-            e_cur, e_alt = runs[pick], runs["plain" if pick == "closure" else "closure"]
+            e_cur, e_alt = errs[pick], errs["plain" if pick == "closure" else "closure"]
         else:
             other = "plain" if pick == "closure" else "closure"
             v = sample.clone()
             closure.step(v, k, use_closure=on[other])
             closure.step(u, k, use_closure=on[pick])
+            ref = judged.result()
             e_cur, e_alt = err_of(u[idx], ref), err_of(v, ref)
         used = pick
         err = float(e_cur.mean())   # the certificate: the sample's mean relative L2 error (the metric's form)
@@ -261,6 +298,8 @@ def run_adaptive(solver, closure: Closure, fine0, coarse_steps: int, segment: in
         prev = err
         if float(e_alt.mean()) < err:
             pick = "plain" if used == "closure" else "closure"
+    if own_judge:
+        judge.close()
     if info["fallback"]:
         f = fine0.clone()
         advance_fine(solver, f, coarse_steps * FACTOR)

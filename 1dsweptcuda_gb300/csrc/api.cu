@@ -269,6 +269,7 @@ int check_status(sw_ctx *ctx, cudaStream_t s) {
     cudaError_t e = cudaMemcpyAsync(&st, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "status readback");
+    if (st == 2) return fail(ctx, SW_ERR_TIMEOUT, "swept kernel: a bulk copy's wait ran out");
     if (st) return fail(ctx, SW_ERR_TIMEOUT, "persistent swept kernel: an inter-block wait expired");
     return SW_OK;
 }
@@ -327,6 +328,7 @@ int run_impl(sw_ctx *ctx, const sw_config &c, const void *ic_host, void *final_h
 
     Plan pl = (c.time_mode == SW_TIME_STEPS) ? plan_steps(c, W, ops->R, ops->S) : plan_reference(c, W, ops->R, ops->S);
     Runner<T> r{ctx, ops, c, make_params<T>(c, k), W, s, primary, ctx->d_work, 0, c.alg == SW_ALG_VARIANT};
+    r.p.status = ctx->d_status;  // bounded waits report here (checked after the run and at snapshots)
     int snaps = 0;
     SW_CUDA(ctx, cudaEventRecord(ctx->k0, s));
     for (size_t i = 0; i < pl.segs.size(); ++i) {
@@ -341,10 +343,8 @@ int run_impl(sw_ctx *ctx, const sw_config &c, const void *ic_host, void *final_h
         if (g.t_snap >= 0 && cb) {
             rc = r.settle(primary);
             if (rc) return rc;
-            if (r.persistent) {
-                rc = check_status<T>(ctx, s);
-                if (rc) return rc;
-            }
+            rc = check_status<T>(ctx, s);
+            if (rc) return rc;
             rc = to_host(ctx, ops, primary, ctx->h_pin, nx, s);
             if (rc) return rc;
             ++snaps;
@@ -358,10 +358,8 @@ int run_impl(sw_ctx *ctx, const sw_config &c, const void *ic_host, void *final_h
     rc = r.settle(primary);
     if (rc) return rc;
     SW_CUDA(ctx, cudaEventRecord(ctx->k1, s));
-    if (r.persistent) {
-        rc = check_status<T>(ctx, s);
-        if (rc) return rc;
-    }
+    rc = check_status<T>(ctx, s);
+    if (rc) return rc;
     if (!device_mode) {
         if (ops->C == 3) {
             SW_CUDA(ctx, ops->unpack(primary, ctx->d_io, nx, s));

@@ -537,6 +537,15 @@ cudaError_t allow_smem() {
     return e;
 }
 
+// The closure calls run on the context's stream, a non-blocking one: order
+// them after the work already queued on the legacy default stream (where a
+// torch caller's default-stream copies of their inputs are).
+int after_legacy(sw_ctx *ctx) {
+    SW_CUDA(ctx, cudaEventRecord(ctx->e0, cudaStreamLegacy));
+    SW_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->e0, 0));
+    return SW_OK;
+}
+
 // Stage theta's layer-2 weights for the forward kernels (stream-ordered before them).
 int stage_w2(sw_ctx *ctx, const float *theta, const uint4 **w2p) {
     if (!ctx->d_w2p) SW_CUDA(ctx, cudaMalloc(&ctx->d_w2p, (size_t)cl::W2P_WORDS * 16));
@@ -556,6 +565,7 @@ int sw_closure_infer(sw_ctx *ctx, const float *theta, const float *u, float *del
     if (rc) return rc;
     if (!theta || !u || !delta) return SW_ERR_ARG;
     SW_CUDA(ctx, cudaSetDevice(ctx->device));
+    if ((rc = after_legacy(ctx)) != SW_OK) return rc;
     SW_CUDA(ctx, allow_smem());
     const int64_t tiles = n / cl::TOUT;
     const uint4 *w2p = nullptr;
@@ -581,6 +591,7 @@ int sw_closure_step(sw_ctx *ctx, const sw_config *coarse, const float *theta, fl
     sw_constants_of(&c, &k);
     const Params<float> p = make_params<float>(c, k);
     SW_CUDA(ctx, cudaSetDevice(ctx->device));
+    if ((rc = after_legacy(ctx)) != SW_OK) return rc;
     SW_CUDA(ctx, allow_smem());
     SW_CUDA(ctx, grow_dev(&ctx->d_work, &ctx->n_work, sizeof(float) * (size_t)n * n_dom));
     float *alt = static_cast<float *>(ctx->d_work), *cur = u;
@@ -619,6 +630,7 @@ int sw_closure_grad(sw_ctx *ctx, const float *theta, const float *u, const float
     if (rc) return rc;
     if (!theta || !u || !target || !grad_and_loss) return SW_ERR_ARG;
     SW_CUDA(ctx, cudaSetDevice(ctx->device));
+    if ((rc = after_legacy(ctx)) != SW_OK) return rc;
     SW_CUDA(ctx, allow_smem());
     const int64_t tiles_per = n / cl::TOUT, n_tiles = tiles_per * n_dom;
     int sms = 0;
@@ -638,6 +650,9 @@ int sw_closure_grad(sw_ctx *ctx, const float *theta, const float *u, const float
 
 int sw_closure_adam(sw_ctx *ctx, float *theta, const float *grad, float *m, float *v, int32_t step, float lr) {
     if (!ctx || !theta || !grad || !m || !v || step < 1) return SW_ERR_ARG;
+    SW_CUDA(ctx, cudaSetDevice(ctx->device));
+    const int rc = after_legacy(ctx);
+    if (rc) return rc;
     const float b1 = 0.9f, b2 = 0.999f;
     const float c1 = 1.0f - std::pow(b1, (float)step), c2 = 1.0f - std::pow(b2, (float)step);
     cl::k_adam<<<(cl::NTRAIN + 255) / 256, 256, 0, ctx->stream>>>(theta, grad, m, v, lr, b1, b2, 1e-8f, c1, c2);
@@ -651,6 +666,7 @@ int sw_closure_train(sw_ctx *ctx, float *theta, const float *inputs, const float
     if (rc) return rc;
     if (!theta || !inputs || !targets || n_samples < 1 || steps < 0) return SW_ERR_ARG;
     SW_CUDA(ctx, cudaSetDevice(ctx->device));
+    if ((rc = after_legacy(ctx)) != SW_OK) return rc;
     // Adam moments and a gradient row live in one allocation owned by this call
     float *buf = nullptr;
     int64_t *rows = nullptr;
@@ -691,6 +707,8 @@ int sw_closure_train(sw_ctx *ctx, float *theta, const float *inputs, const float
 int sw_coarse_grain(sw_ctx *ctx, const double *fine, float *coarse, int64_t n_coarse_total, int32_t factor) {
     if (!ctx || !fine || !coarse || n_coarse_total < 1 || factor < 1) return SW_ERR_ARG;
     SW_CUDA(ctx, cudaSetDevice(ctx->device));
+    const int rc = after_legacy(ctx);
+    if (rc) return rc;
     cl::k_coarse_grain<<<(unsigned)((n_coarse_total + 255) / 256), 256, 0, ctx->stream>>>(fine, coarse,
                                                                                             n_coarse_total, factor);
     SW_CUDA(ctx, cudaGetLastError());

@@ -210,6 +210,79 @@ __device__ __forceinline__ void tile_export(const T *rows, int L, int W, typenam
     for (int i = threadIdx.x; i < W; i += blockDim.x) tile_export_at<P, T>(rows, L, W, sl, sr, i);
 }
 
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// ---- bulk copies between global and shared memory (cp.async.bulk, the
+// copy engine's 1D form), completion of loads tracked by an mbarrier.
+// Addresses and sizes must be multiples of 16 bytes.
+__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ void bulk_load(void *dst_smem, const void *src_global, unsigned bytes, uint64_t *bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(dst_smem)),
+                 "l"(src_global), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_store(void *dst_global, const void *src_smem, unsigned bytes) {
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst_global),
+                 "r"(smem_addr(src_smem)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_store_commit_and_wait() {
+    asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+    asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+}
+// Shared-memory writes of this thread made visible to the copy engine.
+__device__ __forceinline__ void fence_smem_for_bulk() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// Every thread waits for phase 0 of `bar`, up to kBulkWaitNs of %globaltimer
+// (or kBulkWaitNs / 16 polls, should the timer stand still); the block's
+// outcome is uniform.  A wait that runs out sets *status to 2 (when given)
+// and the block returns false, so that its caller returns without touching
+// the tile.  Bulk loads of valid global memory complete in microseconds: the
+// limit only bounds a wait that something else went wrong with.
+constexpr uint64_t kBulkWaitNs = 2000000000ull;
+__device__ __forceinline__ bool bulk_wait(uint64_t *bar, int *status) {
+    const uint64_t t0 = global_ns();
+    uint64_t polls = 0;
+    bool ok = true;
+    while (!mbar_try_wait(bar, 0)) {
+        if (global_ns() - t0 > kBulkWaitNs || ++polls > kBulkWaitNs / 16) {
+            ok = false;
+            break;
+        }
+    }
+    if (__syncthreads_or(!ok)) {
+        if (threadIdx.x == 0 && status) atomicCAS(status, 0, 2);
+        const uint64_t t1 = global_ns();  // the copies in flight write this block's shared memory: wait
+        polls = 0;                        // for them once more, again bounded, before the block leaves
+        while (!mbar_try_wait(bar, 0) && global_ns() - t1 < kBulkWaitNs && ++polls < kBulkWaitNs / 16) {
+        }
+        return false;
+    }
+    return true;
+}
+
 // Aligned 4-value shared-memory loads.
 __device__ __forceinline__ void load4(const float *p, float *w) {
     const float4 v = *reinterpret_cast<const float4 *>(p);
@@ -685,6 +758,84 @@ __device__ __forceinline__ void group_level(const Params<T> &p, T *rows, int TS,
     }
 }
 
+// FP64 KS tiles move their slots (and the up-triangle its state) by bulk
+// copy: with R = 2 cells of 8 bytes, every piece of a tile's import and
+// export starts on a 16-byte boundary in both memories.  One thread issues
+// the copies (4 per tile, or 1 per tile from the state) on one mbarrier; the
+// squares rows that the one-cell path reads are then formed from the
+// imported values, as tile_put forms them.
+#ifndef SW_GROUP_BULK
+#define SW_GROUP_BULK 1  // 0: the per-thread import and export instead (a build for comparison)
+#endif
+template <int P, typename T, int PATH>
+__host__ __device__ constexpr bool group_bulk() {
+    return SW_GROUP_BULK && P == SW_KS && sizeof(T) == 8 && PATH == PATH_CELL;
+}
+
+template <int P, typename T, int MODE, int G>
+__device__ __forceinline__ bool group_bulk_import(const Params<T> &p, const T *state, const T *slots, T *rows, int TS,
+                                                  int L, int W, const int64_t (&base)[G], const int64_t (&hl)[G],
+                                                  const int64_t (&hr)[G]) {
+    constexpr int R = Scheme<P, T>::R;
+    const int h = W >> 1;
+    __shared__ alignas(8) uint64_t bar;
+    if (threadIdx.x == 0) mbar_init(&bar, 1);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned piece = (unsigned)(h * sizeof(T));
+        mbar_expect_tx(&bar, (unsigned)(G * W * (MODE == MODE_UP ? 1 : 2) * sizeof(T)));
+#pragma unroll
+        for (int k = 0; k < G; ++k) {
+            T *rk = rows + k * TS;
+            if constexpr (MODE == MODE_UP) {
+                bulk_load(rk + R, state + base[k], 2 * piece, &bar);  // row 0, cells 0 .. W-1
+            } else {
+                const T *sl = slots + hl[k] * W, *sr = slots + hr[k] * W;
+                bulk_load(rk + R, sl, piece, &bar);                  // row 0, cells 0 .. h-1
+                bulk_load(rk + L, sl + h, piece, &bar);              // row 1, cells -R .. h-R-1
+                bulk_load(rk + R + h, sr, piece, &bar);              // row 0, cells h .. W-1
+                bulk_load(rk + L + h + 2 * R, sr + h, piece, &bar);  // row 1, cells h+R .. W+R-1
+            }
+        }
+    }
+    if (!bulk_wait(&bar, p.status)) return false;
+    // squares of the imported cells (rows 2 and 3)
+    for (int i = threadIdx.x; i < G * W; i += blockDim.x) {
+        const int k = i / W, x = i - k * W;
+        T *rk = rows + k * TS;
+        const T v0 = rk[R + x];
+        rk[2 * L + R + x] = ml(v0, v0);
+        if constexpr (MODE != MODE_UP) {
+            const int c = x < h ? x - R : x + R;  // row 1's imported cells
+            const T v1 = rk[L + R + c];
+            rk[3 * L + R + c] = ml(v1, v1);
+        }
+    }
+    return true;
+}
+
+template <int P, typename T, int G>
+__device__ __forceinline__ void group_bulk_export(T *slots, T *rows, int TS, int L, int W, const int64_t (&hl)[G],
+                                                  const int64_t (&hr)[G]) {
+    constexpr int R = Scheme<P, T>::R;
+    const int h = W >> 1;
+    fence_smem_for_bulk();  // this thread's row writes, visible to the copy engine
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned piece = (unsigned)(h * sizeof(T));
+#pragma unroll
+        for (int k = 0; k < G; ++k) {
+            const T *rk = rows + k * TS;
+            T *sl = slots + hl[k] * W, *sr = slots + hr[k] * W;
+            bulk_store(sl, rk + R, piece);                  // row 0, cells 0 .. h-1
+            bulk_store(sl + h, rk + L + 2 * R, piece);      // row 1, cells R .. h+R-1
+            bulk_store(sr, rk + R + h, piece);              // row 0, cells h .. W-1
+            bulk_store(sr + h, rk + L + h, piece);          // row 1, cells h-R .. W-R-1
+        }
+        bulk_store_commit_and_wait();  // complete before the block's shared memory goes
+    }
+}
+
 template <int P, typename T, int MODE, int G, int PATH>
 __device__ __forceinline__ void swept_tile_group(const Params<T> &p, T *__restrict__ state, T *__restrict__ slots,
                                                  T *rows, const int W, const int phase, const int64_t t0) {
@@ -702,10 +853,14 @@ __device__ __forceinline__ void swept_tile_group(const Params<T> &p, T *__restri
         e[k] = tile_ends(base[k], nx, W, R);
     }
     // import / export: element i of the block is element i % W of tile i / W
-    for (int i = threadIdx.x; i < G * W; i += blockDim.x) {
-        const int k = i / W, x = i - k * W;
-        if constexpr (MODE == MODE_UP) tile_put<P, T>(rows + k * TS, L, 0, x, state[base[k] + x]);
-        else tile_import_at<P, T>(rows + k * TS, L, W, slots + hl[k] * W, slots + hr[k] * W, x);
+    if constexpr (group_bulk<P, T, PATH>()) {
+        if (!group_bulk_import<P, T, MODE, G>(p, state, slots, rows, TS, L, W, base, hl, hr)) return;
+    } else {
+        for (int i = threadIdx.x; i < G * W; i += blockDim.x) {
+            const int k = i / W, x = i - k * W;
+            if constexpr (MODE == MODE_UP) tile_put<P, T>(rows + k * TS, L, 0, x, state[base[k] + x]);
+            else tile_import_at<P, T>(rows + k * TS, L, W, slots + hl[k] * W, slots + hr[k] * W, x);
+        }
     }
     __syncthreads();
     if constexpr (MODE != MODE_UP) {  // down part, two levels per iteration (H is even)
@@ -730,10 +885,14 @@ __device__ __forceinline__ void swept_tile_group(const Params<T> &p, T *__restri
             __syncthreads();
         }
         group_level<P, T, G, PATH>(p, rows, TS, L, 1, u * R, W - u * R, e);  // u = H - 1
-        __syncthreads();
-        for (int i = threadIdx.x; i < G * W; i += blockDim.x) {
-            const int k = i / W, x = i - k * W;
-            tile_export_at<P, T>(rows + k * TS, L, W, slots + hl[k] * W, slots + hr[k] * W, x);
+        if constexpr (group_bulk<P, T, PATH>()) {
+            group_bulk_export<P, T, G>(slots, rows, TS, L, W, hl, hr);
+        } else {
+            __syncthreads();
+            for (int i = threadIdx.x; i < G * W; i += blockDim.x) {
+                const int k = i / W, x = i - k * W;
+                tile_export_at<P, T>(rows + k * TS, L, W, slots + hl[k] * W, slots + hr[k] * W, x);
+            }
         }
     }
 }

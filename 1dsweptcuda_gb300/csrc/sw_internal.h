@@ -23,6 +23,7 @@ struct Params {
     int ks_form;               // KS: how c4, d2, d4 enter the right-hand side (enum KsForm)
     int d2_e;                  // KS_POW2: d2 = 2^d2_e
     T nz;                      // -0.0, the addend that makes an fma a plain product (paired FP32 path)
+    int *status;               // device word a kernel sets when a bounded wait runs out (may be null)
 };
 
 // KS right-hand-side forms.  KS_POW2: c4, d2, d4 are exact powers of two, so

@@ -203,6 +203,7 @@ class Solver:
     """One device context (stream + reusable work buffers)."""
 
     def __init__(self, device: int = 0):
+        self.device = device
         self._lib = library()
         self._ctx = C.c_void_p()
         rc = self._lib.sw_ctx_create(device, C.byref(self._ctx))

@@ -43,7 +43,7 @@ enum sw_status {
     SW_ERR_CUDA = -4,        /* a CUDA call or kernel failed */
     SW_ERR_NOMEM = -5,       /* device or pinned host allocation failed */
     SW_ERR_IO = -6,          /* output file could not be opened or written */
-    SW_ERR_TIMEOUT = -7,     /* a bounded inter-block wait expired; state not valid */
+    SW_ERR_TIMEOUT = -7,     /* a kernel's bounded wait (inter-block flags, a bulk copy) ran out; state not valid */
     SW_ERR_UNSUPPORTED = -8, /* valid request this library does not provide */
     SW_ERR_CALLBACK = -9,    /* the snapshot callback asked to stop */
     SW_ERR_USAGE = -10       /* too few command-line arguments (argc < 8) */
@@ -190,7 +190,9 @@ int sw_run_device(sw_ctx *ctx, const sw_config *cfg, void *state_dev, void *stre
  * split into parts that run their passes as periodic domains of their own
  * therefore needs only that slot (before and after each phase-1 pass) and
  * those cells (after a phase-1 down-triangle) moved between neighbours; the
- * package's split.py does this across devices or processes. */
+ * package's split.py does this across devices or processes.  The kernels'
+ * bounded waits (on their bulk copies) are not reported by this call, which
+ * does not wait for them; sw_run_device reports them as SW_ERR_TIMEOUT. */
 int sw_swept_pass(sw_ctx *ctx, const sw_config *cfg, int32_t mode, int32_t phase, void *state_dev, void *slots_dev,
                   void *stream);
 
@@ -252,8 +254,9 @@ int sw_query_tuning(sw_ctx *ctx, const sw_config *cfg, int32_t n_domains, const 
  * pass; the 32 -> 32 layer runs on the tensor cores (BF16 x BF16,
  * FP32 accumulation), forward and backward.  Every array argument is a
  * device pointer; states are float32 domains of n cells (n a multiple of
- * 128) stored one after another.  The calls run on the context's stream and
- * return when done. */
+ * 128) stored one after another.  The calls run on the context's stream,
+ * after the work already queued on the legacy default stream, and return
+ * when done. */
 #define SW_CLOSURE_PARAMS 5506
 /* delta = f(u) for n_dom domains. */
 int sw_closure_infer(sw_ctx *ctx, const float *theta, const float *u, float *delta, int32_t n_dom, int64_t n);
