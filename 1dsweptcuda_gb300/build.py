@@ -27,12 +27,16 @@ INCLUDE = ROOT / "include"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # -fmad=false: no contraction anywhere; the stencils also spell every
 # operation with a round-to-nearest intrinsic, so they never depend on it.
+# -ffp-contract=off for the host compiler: the host tile (host_tile.cu) runs the
+# stencils on the CPU, where each operation must round on its own.
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC",
+                     "-Xcompiler", "-ffp-contract=off",
                      "-Xptxas", "-warn-spills", "-I", str(INCLUDE)]
 # Extra nvcc flags from the environment (e.g. -DSW_EULER_MIN_BLOCKS=3, a tuning macro).
 # A change of them is not tracked: rebuild with --force.
 NVCC_FLAGS += os.environ.get("SW_NVCC_EXTRA", "").split()
-CU_SOURCES = ["k_heat.cu", "k_ks.cu", "k_ks_div.cu", "k_euler.cu", "api.cu", "batch.cu", "noalloc.cu", "closure.cu", "diag.cu"]
+CU_SOURCES = ["k_heat.cu", "k_ks.cu", "k_ks_div.cu", "k_euler.cu", "api.cu", "batch.cu", "noalloc.cu", "closure.cu", "diag.cu",
+              "host_tile.cu"]
 CPP_SOURCES = ["cli.cpp"]
 HEADERS = ["engine.cuh", "stencils.cuh", "persistent.cuh", "sw_internal.h", "ctx.h", "exact_int.h"]
 PROGRAMS = [(p, pi, q, qi) for pi, p in enumerate(("Heat", "KS", "Euler")) for q, qi in (("Single", 4), ("Double", 8))]

@@ -143,11 +143,13 @@ def fine_ensemble(n_traj: int, seed: int):
     return torch.from_numpy(u.reshape(n_traj, FINE_NX)).cuda()
 
 
-def advance_fine(solver, fine, steps: int):
+def advance_fine(solver, fine, steps: int, stream: int = 0):
+    """Advance the (n, 4096) FP64 fine states by `steps` fine steps on the
+    solver's context, ordered after `stream` (0: the legacy default stream)."""
     sw = _sw()
     n_traj = fine.shape[0]
     nx = np.full(n_traj, FINE_NX, dtype=np.int64)
-    solver.run_batch_device(fine_config(sw, steps), nx, fine.data_ptr())
+    solver.run_batch_device(fine_config(sw, steps), nx, fine.data_ptr(), stream)
 
 
 def make_training_data(solver, closure: Closure, n_traj: int, snapshots: int, interval: int, seed: int = 7,
@@ -183,28 +185,6 @@ def rel_l2(a, b) -> float:
     return float((num / den).mean().item())
 
 
-class _Background:
-    """fn() run in a thread; result() joins it and returns (or raises) its outcome."""
-
-    def __init__(self, fn):
-        import threading
-        self._out, self._err = None, None
-
-        def body():
-            try:
-                self._out = fn()
-            except BaseException as e:  # re-raised in result()
-                self._err = e
-        self._t = threading.Thread(target=body, daemon=True)
-        self._t.start()
-
-    def result(self):
-        self._t.join()
-        if self._err is not None:
-            raise self._err
-        return self._out
-
-
 def shadow_domains(n_dom: int, every: int, seed: int = 0):
     """The judge's sample: one domain in each run of `every`, at a seeded offset."""
     torch = _torch()
@@ -222,10 +202,11 @@ def run_adaptive(solver, closure: Closure, fine0, coarse_steps: int, segment: in
     advances the exact fine state of a seeded sample of the domains (one in
     `shadow_every`) alongside the coarse run, on the context `judge` (default:
     one made for the call; pass one to keep its captured graphs warm across
-    calls), in a thread, so that it overlaps the coarse runs.  Before the first
-    segment both coarse variants advance the sample and the one nearer the
-    coarse-grained shadow (mean relative L2 error over the sample) is
-    picked; after that the ensemble runs each segment with the current pick
+    calls), ahead of the coarse runs of each segment (its few launches run
+    alone faster than beside the ensemble's).  In the first segment both
+    coarse variants advance the sample and the one nearer the coarse-grained
+    shadow (mean relative L2 error over the sample) advances the ensemble;
+    after that the ensemble runs each segment with the current pick
     while the other variant advances the sample alone, and the pick changes
     when the other variant ends the segment nearer the shadow -- so the
     closure is used exactly where it beats the plain step.  The sample's
@@ -239,7 +220,7 @@ def run_adaptive(solver, closure: Closure, fine0, coarse_steps: int, segment: in
     the segments run with the closure and plain, whether it fell back, the
     sample's final error (max and mean) and a per-segment log."""
     torch = _torch()
-    own_judge = judge is None or judge is solver   # a context serves one host thread at a time
+    own_judge = judge is None or judge is solver   # the judge keeps graphs of its own shape
     if own_judge:
         judge = _sw().Solver(solver.device)
     u = coarse_grain(solver, fine0)
@@ -262,27 +243,24 @@ def run_adaptive(solver, closure: Closure, fine0, coarse_steps: int, segment: in
     done, prev, pick = 0, 0.0, None
     while done < coarse_steps:
         k = min(segment, coarse_steps - done)
-        sample = u[idx].contiguous()
-        # the judge's fine segment runs on its own context and stream, in a thread (the
-        # library releases the interpreter while it waits), overlapping the coarse runs
-        judged = _Background(lambda: (advance_fine(judge, shadow, k * FACTOR), coarse_grain(judge, shadow))[1])
+        # the judge's segment first: its few launches run alone on the GPU (run beside the
+        # ensemble's thousands of blocks, each of them waited for an SM slot)
+        advance_fine(judge, shadow, k * FACTOR)
+        ref = coarse_grain(judge, shadow)
         if pick is None:  # first segment: both variants on the sample, then the ensemble with the better one
             runs = {}
             for name in on:
-                v = sample.clone()
+                v = u[idx].contiguous()
                 closure.step(v, k, use_closure=on[name])
-                runs[name] = v
-            ref = judged.result()
-            errs = {name: err_of(v, ref) for name, v in runs.items()}
-            pick = min(errs, key=lambda nm: float(errs[nm].mean()))
+                runs[name] = err_of(v, ref)
+            pick = min(runs, key=lambda nm: float(runs[nm].mean()))
             closure.step(u, k, use_closure=on[pick])
-            e_cur, e_alt = errs[pick], errs["plain" if pick == "closure" else "closure"]
+            e_cur, e_alt = runs[pick], runs["plain" if pick == "closure" else "closure"]
         else:
             other = "plain" if pick == "closure" else "closure"
-            v = sample.clone()
+            v = u[idx].contiguous()
             closure.step(v, k, use_closure=on[other])
             closure.step(u, k, use_closure=on[pick])
-            ref = judged.result()
             e_cur, e_alt = err_of(u[idx], ref), err_of(v, ref)
         used = pick
         err = float(e_cur.mean())   # the certificate: the sample's mean relative L2 error (the metric's form)
@@ -489,8 +467,8 @@ if __name__ == "__main__":
     if a.bench_step:
         print(json.dumps(bench_step(steps=a.bench_step)))
         sys.exit(0)
-    res = evaluate(a.train_traj, a.snapshots, a.eval, [float(t) for t in a.ic_horizons.split(",")],
-                   [float(t) for t in a.chaos_horizons.split(",")], a.train_steps, tau=a.tau, segment=a.segment,
+    res = evaluate(a.train_traj, a.snapshots, a.eval, [float(t) for t in a.ic_horizons.split(",") if t],
+                   [float(t) for t in a.chaos_horizons.split(",") if t], a.train_steps, tau=a.tau, segment=a.segment,
                    shadow_every=a.shadow_every, decay=a.decay)
     print(json.dumps(res, indent=1))
     if a.json:

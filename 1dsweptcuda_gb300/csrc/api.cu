@@ -220,6 +220,39 @@ struct Runner {
     void *alt;  // classic work buffer
     int64_t launches = 0;
     bool persistent;
+    bool host_tile = false;  // SW_FLAG_HOST_TILE: phase-1 passes leave their wrapping tile to the host
+
+    // One launch-per-pass pass.  With the host tile, a phase-1 pass launches every
+    // tile but the last (the one that wraps from cell nx-1 to 0: the launch covers
+    // nx - W cells while Params::nx stays the domain's) and the host computes that
+    // tile meanwhile from its two slots, copied down before the launch and back
+    // after it on the same stream.
+    int pass(int mode, int phase) {
+        const int64_t nx = cfg.nx;
+        if (!host_tile || phase == 0) {
+            SW_CUDA(ctx, ops->swept(&p, mode, phase, cur, ctx->d_slots, nx, W, cfg.threads, s));
+            return SW_OK;
+        }
+        const size_t wb = ops->cell * (size_t)W, hb = wb / 2;
+        char *slots = static_cast<char *>(ctx->d_slots), *state = static_cast<char *>(cur);
+        char *dl = slots + (size_t)(nx / (W / 2) - 1) * wb, *dr = slots;
+        char *h = static_cast<char *>(ctx->h_tile);  // [slot l: W][slot r: W][state first: W/2][state last: W/2]
+        SW_CUDA(ctx, cudaMemcpyAsync(h, dl, wb, cudaMemcpyDeviceToHost, s));
+        SW_CUDA(ctx, cudaMemcpyAsync(h + wb, dr, wb, cudaMemcpyDeviceToHost, s));
+        SW_CUDA(ctx, cudaEventRecord(ctx->tile_ready, s));
+        if (nx > W) SW_CUDA(ctx, ops->swept(&p, mode, 1, cur, ctx->d_slots, nx - W, W, cfg.threads, s));
+        SW_CUDA(ctx, cudaEventSynchronize(ctx->tile_ready));
+        host_tile_run(cfg.problem, cfg.precision, &p, mode, h, h + wb, h + 2 * wb, h + 2 * wb + hb, W);
+        if (mode == MODE_DIAMOND) {
+            SW_CUDA(ctx, cudaMemcpyAsync(dl, h, wb, cudaMemcpyHostToDevice, s));
+            SW_CUDA(ctx, cudaMemcpyAsync(dr, h + wb, wb, cudaMemcpyHostToDevice, s));
+        } else {
+            SW_CUDA(ctx, cudaMemcpyAsync(state, h + 2 * wb, hb, cudaMemcpyHostToDevice, s));
+            SW_CUDA(ctx, cudaMemcpyAsync(state + (size_t)(nx - W / 2) * ops->cell, h + 2 * wb + hb, hb,
+                                         cudaMemcpyHostToDevice, s));
+        }
+        return SW_OK;
+    }
 
     int classic_steps(int64_t n) {
         const int64_t nx = cfg.nx;
@@ -246,11 +279,11 @@ struct Runner {
             ++launches;
             return SW_OK;
         }
-        SW_CUDA(ctx, ops->swept(&p, MODE_UP, 0, cur, ctx->d_slots, nx, W, cfg.threads, s));
-        for (int64_t d = 1; d <= nd; ++d) SW_CUDA(ctx, ops->swept(&p, MODE_DIAMOND, (int)(d & 1), cur, ctx->d_slots, nx, W, cfg.threads, s));
-        SW_CUDA(ctx, ops->swept(&p, MODE_DOWN, down_phase, cur, ctx->d_slots, nx, W, cfg.threads, s));
+        int rc = pass(MODE_UP, 0);
+        for (int64_t d = 1; d <= nd && rc == SW_OK; ++d) rc = pass(MODE_DIAMOND, (int)(d & 1));
+        if (rc == SW_OK) rc = pass(MODE_DOWN, down_phase);
         launches += nd + 2;
-        return SW_OK;
+        return rc;
     }
 
     // cur back into the primary state buffer (Heat classic leaves it in alt after odd counts)
@@ -327,7 +360,14 @@ int run_impl(sw_ctx *ctx, const sw_config &c, const void *ic_host, void *final_h
     }
 
     Plan pl = (c.time_mode == SW_TIME_STEPS) ? plan_steps(c, W, ops->R, ops->S) : plan_reference(c, W, ops->R, ops->S);
-    Runner<T> r{ctx, ops, c, make_params<T>(c, k), W, s, primary, ctx->d_work, 0, c.alg == SW_ALG_VARIANT};
+    const bool host_tile = (c.flags & SW_FLAG_HOST_TILE) != 0;
+    if (host_tile) {
+        SW_CUDA(ctx, grow_pinned(&ctx->h_tile, &ctx->n_tile, ops->cell * (size_t)W * 3));
+        if (!ctx->tile_ready) SW_CUDA(ctx, cudaEventCreateWithFlags(&ctx->tile_ready, cudaEventDisableTiming));
+    }
+    Runner<T> r{ctx, ops, c, make_params<T>(c, k), W, s, primary, ctx->d_work, 0,
+                c.alg == SW_ALG_VARIANT && !host_tile};
+    r.host_tile = host_tile;
     r.p.status = ctx->d_status;  // bounded waits report here (checked after the run and at snapshots)
     int snaps = 0;
     SW_CUDA(ctx, cudaEventRecord(ctx->k0, s));
@@ -454,6 +494,8 @@ int sw_ctx_destroy(sw_ctx *c) {
     for (void *b : bufs)
         if (b) cudaFree(b);
     if (c->h_pin) cudaFreeHost(c->h_pin);
+    if (c->h_tile) cudaFreeHost(c->h_tile);
+    if (c->tile_ready) cudaEventDestroy(c->tile_ready);
     if (c->batch.d_tables) cudaFree(c->batch.d_tables);
     if (c->graph.exec) cudaGraphExecDestroy(c->graph.exec);
     cudaEvent_t evs[] = {c->e0, c->e1, c->k0, c->k1};
@@ -490,8 +532,12 @@ int sw_validate(const sw_config *c) {
     if (c->alg < SW_ALG_CLASSIC || c->alg > SW_ALG_SELFTEST) return SW_ERR_ARG;
     if (c->alg == SW_ALG_SELFTEST && c->problem != SW_KS) return SW_ERR_ARG;
     if (c->time_mode != SW_TIME_REFERENCE && c->time_mode != SW_TIME_STEPS) return SW_ERR_ARG;
-    if ((c->flags & ~SW_FLAG_KS_DIVIDE) != 0) return SW_ERR_ARG;
+    if ((c->flags & ~(SW_FLAG_KS_DIVIDE | SW_FLAG_HOST_TILE)) != 0) return SW_ERR_ARG;
     if ((c->flags & SW_FLAG_KS_DIVIDE) && c->problem != SW_KS) return SW_ERR_ARG;
+    if (c->flags & SW_FLAG_HOST_TILE) {  // the hybrid variant: swept passes, not with the dividing KS build
+        const bool alg_ok = c->alg == SW_ALG_SWEPT || (c->alg == SW_ALG_VARIANT && c->problem != SW_KS);
+        if (!alg_ok || (c->flags & SW_FLAG_KS_DIVIDE)) return SW_ERR_ARG;
+    }
     const int bc = resolved_bc(*c);
     if (c->problem == SW_HEAT && bc != SW_BC_MIRROR && bc != SW_BC_PERIODIC) return SW_ERR_ARG;
     if (c->problem == SW_KS && bc != SW_BC_PERIODIC) return SW_ERR_ARG;
@@ -631,6 +677,7 @@ int sw_swept_pass(sw_ctx *ctx, const sw_config *cfg, int32_t mode, int32_t phase
     int rc = sw_validate(cfg);
     if (rc) return fail(ctx, rc, std::string("invalid configuration: ") + sw_strerror(rc));
     if (cfg->alg != SW_ALG_SWEPT) return fail(ctx, SW_ERR_UNSUPPORTED, "a swept pass needs alg 1");
+    if (cfg->flags & SW_FLAG_HOST_TILE) return fail(ctx, SW_ERR_UNSUPPORTED, "the host tile is a run's, not a pass's");
     if (mode < MODE_UP || mode > MODE_DOWN || (phase != 0 && phase != 1) || (mode == MODE_UP && phase != 0))
         return fail(ctx, SW_ERR_ARG, "mode must be 0 (up, phase 0), 1 (diamond) or 2 (down); phase 0 or 1");
     if (!state_dev || !slots_dev) return fail(ctx, SW_ERR_ARG, "null device state or slots");

@@ -288,6 +288,13 @@ int cli(int problem, int argc, char **argv) {
         const char *d = std::getenv("SWEPT1D_KS_DIVIDE");
         if (d && *d && std::strcmp(d, "0") != 0) cfg.flags |= SW_FLAG_KS_DIVIDE;
     }
+    // The reference's alg 2 for Heat and Euler is its hybrid variant (the split
+    // node on the CPU); here alg 2 is the GPU-only persistent kernel unless
+    // SWEPT1D_HOST_TILE asks for the host tile (alg 1 or 2).
+    {
+        const char *t = std::getenv("SWEPT1D_HOST_TILE");
+        if (t && *t && std::strcmp(t, "0") != 0) cfg.flags |= SW_FLAG_HOST_TILE;
+    }
     std::cout.precision(10);
 
     sw_constants k;

@@ -114,6 +114,9 @@ struct sw_ctx {
     void *d_w2p = nullptr;  // closure layer-2 weights, BF16, in the kernels' shared-memory layout
     void *h_pin = nullptr;
     size_t n_pin = 0;
+    void *h_tile = nullptr;         // the hybrid variant's host tile: its two slots and two state pieces
+    size_t n_tile = 0;
+    cudaEvent_t tile_ready = nullptr;  // the host tile's slots have arrived in h_tile
     sw::BatchTables batch;
     sw::GraphCache graph;
     sw::TuneCache tune;

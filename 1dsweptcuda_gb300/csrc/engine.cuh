@@ -108,10 +108,10 @@ __device__ __forceinline__ Ends tile_ends(int64_t base, int64_t nx, int W, int R
 }
 
 // One Heat / KS sub-step of parity `par` (1: predictor / odd Heat step; 0:
-// corrector / even Heat step) at tile cell x.  (Euler levels run euler_level_tile.)
+// corrector / even Heat step) at tile cell x.  (Euler levels run euler_level_tile / _warp.)
 template <int P, typename T>
 __device__ __forceinline__ void tile_point(const Params<T> &p, T *rows, int L, int par, int x, Ends e) {
-    static_assert(P != SW_EULER, "Euler tile levels compute each interface once (euler_level_tile)");
+    static_assert(P != SW_EULER, "Euler tile levels run euler_level_tile / euler_level_warp");
     constexpr int R = Scheme<P, T>::R;
     const T *src = rows + (par ^ 1) * L + R;
     T *dst = rows + par * L + R;
@@ -134,13 +134,14 @@ __device__ __forceinline__ void tile_point(const Params<T> &p, T *rows, int L, i
     }
 }
 
-// Euler tiles also keep, per level, the interface terms of euler_level_tile:
-// the pressure differences D and the flux F and dissipation S (3 components
-// each) of every interface, 7 values per row position.
+// FP64 Euler tiles also keep, per level, the interface terms of
+// euler_level_tile: the pressure differences D and the flux F and dissipation
+// S (3 components each) of every interface, 7 values per row position.
 constexpr int kEulerIfaceArrays = 7;
 template <int P, typename T>
 __host__ __device__ constexpr size_t swept_smem_bytes(int W) {
-    return sizeof(T) * ((size_t)tile_rows<P>() * Scheme<P, T>::C + (P == SW_EULER ? kEulerIfaceArrays : 0)) *
+    return sizeof(T) *
+           ((size_t)tile_rows<P>() * Scheme<P, T>::C + (P == SW_EULER && sizeof(T) == 8 ? kEulerIfaceArrays : 0)) *
            (size_t)row_stride(W);
 }
 
@@ -389,6 +390,42 @@ __device__ __forceinline__ Q3<T> shfl_down3(Q3<T> v, int d) {
               __shfl_down_sync(0xffffffffu, v.z, d));
 }
 
+// FP32 Euler levels keep the warp scheme: an FP32 tile is bound by instruction
+// issue, where three passes with a barrier after each cost more than the 3 lanes
+// of 32 they save (0.95x against 1.01x of classic, nx = 2^22).  Values read
+// past W + R - 1 (clamped) only reach lanes whose cells are not stored.
+template <typename T>
+__device__ __forceinline__ void euler_level_warp(const Params<T> &p, T *rows, int L, int W, int par, int lo, int hi,
+                                                 Ends e) {
+    constexpr int R = Scheme<SW_EULER, T>::R;
+    const T *src = rows + (par ^ 1) * 3 * L + R;
+    T *dst = rows + par * 3 * L + R;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    const T scale = par ? ml(T(0.25), p.dtdx) : ml(T(0.5), p.dtdx);
+    for (int s0 = lo + warp * kEulerCellsPerWarp; s0 < hi; s0 += nwarp * kEulerCellsPerWarp) {
+        const int b = s0 + lane;
+        Q3<T> c[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int x = min(b - 2 + k, W + R - 1);
+            c[k] = q3(src[x], src[L + x], src[2 * L + x]);
+        }
+        // zero across the domain's ends (the reference's edge flags, Euler1D_SweptShared.cu:311-335)
+        const T D = (b - 1 == e.first || b - 2 == e.last) ? T(0) : eu_pdiff(c[0], c[1]);
+        const T D1 = __shfl_down_sync(0xffffffffu, D, 1), D2 = __shfl_down_sync(0xffffffffu, D, 2);
+        Q3<T> F, S;
+        eu_iface(p, c[0], c[1], c[2], c[3], D, D1, D2, F, S);
+        const Q3<T> Fr = shfl_down3(F, 1), Sr = shfl_down3(S, 1);
+        if (lane < kEulerCellsPerWarp && b < hi && b != e.first && b != e.last) {
+            const Q3<T> base = par ? c[2] : q3(dst[b], dst[L + b], dst[2 * L + b]);
+            const Q3<T> o = qadd(base, qscale(scale, eu_combine(F, S, Fr, Sr)));
+            dst[b] = o.x;
+            dst[L + b] = o.y;
+            dst[2 * L + b] = o.z;
+        }
+    }
+}
+
 // Euler sub-step over tile cells [lo, hi) of a swept tile, every interface
 // computed once, in three passes of the whole block through shared memory
 // (xs: kEulerIfaceArrays rows of L values after the tile rows):
@@ -448,7 +485,7 @@ __device__ __forceinline__ void euler_level_tile(const Params<T> &p, T *rows, in
 // Which cell mapping a kernel carries: PATH_ANY picks at run time (blockDim.x
 // * 4 == W: 4 cells per thread), PATH_CELL and PATH_SPAN4 hold only one, so a
 // kernel does not pay the registers of a path it never runs.  Euler always
-// runs euler_level_tile.
+// runs euler_level_tile (FP64) or euler_level_warp (FP32).
 enum TilePath { PATH_ANY = 0, PATH_CELL = 1, PATH_SPAN4 = 2 };
 
 // Heat / KS cells [lo, hi) of one level, one per thread from the lowest thread,
@@ -470,7 +507,8 @@ template <int P, typename T, int PATH>
 __device__ __forceinline__ void tile_level(const Params<T> &p, T *rows, int L, int W, int par, int lo, int hi,
                                            Ends e) {
     if constexpr (P == SW_EULER) {
-        euler_level_tile<T>(p, rows, L, par, lo, hi, e);
+        if constexpr (sizeof(T) == 8) euler_level_tile<T>(p, rows, L, par, lo, hi, e);
+        else euler_level_warp<T>(p, rows, L, W, par, lo, hi, e);
     } else if constexpr (PATH == PATH_SPAN4) {
         tile_span4<P, T>(p, rows, L, par, lo, hi, e, (int)threadIdx.x);
     } else if constexpr (PATH == PATH_CELL) {
@@ -585,7 +623,7 @@ __device__ __forceinline__ void swept_tile(const Params<T> &p, typename Scheme<P
 
 // One swept pass over all tiles of one domain; block = one tile.
 // FP32 four-cells-per-thread blocks ask for 2048 resident threads per SM (32 registers).
-// Euler tiles (256 threads) ask for SW_EULER_MIN_BLOCKS blocks per SM: an
+// FP64 Euler tiles (256 threads) ask for SW_EULER_MIN_BLOCKS blocks per SM: an
 // Euler level is three passes with a barrier after each, and other blocks'
 // warps keep the FP64 pipe busy through them.
 #ifndef SW_EULER_MIN_BLOCKS
@@ -593,7 +631,7 @@ __device__ __forceinline__ void swept_tile(const Params<T> &p, typename Scheme<P
 #endif
 template <int P, typename T, int PATH>
 constexpr int swept_min_blocks() {
-    if (P == SW_EULER) return SW_EULER_MIN_BLOCKS;
+    if (P == SW_EULER) return sizeof(T) == 8 ? SW_EULER_MIN_BLOCKS : 1;
     return (PATH == PATH_SPAN4 && sizeof(T) == 4) ? 2048 / Scheme<P, T>::MAXT : 1;
 }
 template <int P, typename T, int MODE, int PATH>
@@ -839,7 +877,7 @@ __device__ __forceinline__ void group_bulk_export(T *slots, T *rows, int TS, int
 template <int P, typename T, int MODE, int G, int PATH>
 __device__ __forceinline__ void swept_tile_group(const Params<T> &p, T *__restrict__ state, T *__restrict__ slots,
                                                  T *rows, const int W, const int phase, const int64_t t0) {
-    static_assert(P != SW_EULER, "Euler levels run euler_level_tile");
+    static_assert(P != SW_EULER, "Euler tiles are not grouped");
     constexpr int R = Scheme<P, T>::R;
     const int L = row_stride(W), h = W >> 1, H = W / (2 * R), TS = tile_rows<P>() * L;
     const int64_t nx = p.nx, nhalf = nx / h;
@@ -1013,10 +1051,11 @@ __device__ __forceinline__ void ks_warp4_level(const Params<T> &p, int par, int 
 
 template <typename T, int MODE>
 __global__ void __launch_bounds__(32 * kKsWarpTilesPerBlock)
-    k_swept_ks_warp(const Params<T> p, T *__restrict__ state, T *__restrict__ slots, const int phase) {
+    k_swept_ks_warp(const Params<T> p, T *__restrict__ state, T *__restrict__ slots, const int phase,
+                    const int64_t ntile) {
     constexpr int W = kKsWarpTile, h = W / 2, R = 2, H = W / (2 * R);
     const int lane = threadIdx.x & 31, c0 = 4 * lane;
-    const int64_t nx = p.nx, ntile = nx / W, nhalf = nx / h;
+    const int64_t nx = p.nx, nhalf = nx / h;  // ntile: the tiles launched (all, or all but the wrapping one)
     const int64_t t = (int64_t)blockIdx.x * kKsWarpTilesPerBlock + (threadIdx.x >> 5);
     if (t >= ntile) return;  // whole warps: t is the same for the 32 lanes
     const int64_t base = t * W + (int64_t)phase * h;
@@ -1095,9 +1134,9 @@ cudaError_t launch_swept_ks_warp(const Params<T> &p, int mode, int phase, T *st,
     const unsigned grid = (unsigned)((ntile + kKsWarpTilesPerBlock - 1) / kKsWarpTilesPerBlock);
     const int threads = 32 * kKsWarpTilesPerBlock;
     switch (mode) {
-    case MODE_UP: k_swept_ks_warp<T, MODE_UP><<<grid, threads, 0, s>>>(p, st, sl, phase); break;
-    case MODE_DIAMOND: k_swept_ks_warp<T, MODE_DIAMOND><<<grid, threads, 0, s>>>(p, st, sl, phase); break;
-    default: k_swept_ks_warp<T, MODE_DOWN><<<grid, threads, 0, s>>>(p, st, sl, phase); break;
+    case MODE_UP: k_swept_ks_warp<T, MODE_UP><<<grid, threads, 0, s>>>(p, st, sl, phase, ntile); break;
+    case MODE_DIAMOND: k_swept_ks_warp<T, MODE_DIAMOND><<<grid, threads, 0, s>>>(p, st, sl, phase, ntile); break;
+    default: k_swept_ks_warp<T, MODE_DOWN><<<grid, threads, 0, s>>>(p, st, sl, phase, ntile); break;
     }
     return cudaGetLastError();
 }

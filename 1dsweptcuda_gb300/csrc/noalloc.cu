@@ -113,7 +113,8 @@ extern "C" int sw_run_device_noalloc(const sw_config *cfg, void *state_dev, void
     if (!cfg || !state_dev) return SW_ERR_ARG;
     int rc = sw_validate(cfg);
     if (rc) return rc;
-    if (cfg->alg != SW_ALG_SWEPT || cfg->time_mode != SW_TIME_STEPS) return SW_ERR_UNSUPPORTED;
+    if (cfg->alg != SW_ALG_SWEPT || cfg->time_mode != SW_TIME_STEPS || (cfg->flags & SW_FLAG_HOST_TILE))
+        return SW_ERR_UNSUPPORTED;
     if (scratch_need(ops_for(cfg->problem, cfg->precision, cfg->flags), cfg->nx) > (size_t)SW_NOALLOC_SCRATCH_BYTES)
         return SW_ERR_SIZE;
     if (!on_current_device(state_dev)) return SW_ERR_ARG;

@@ -9,6 +9,8 @@
 
 #include <cuda_runtime.h>
 
+#include <cmath>
+
 #include "exact_int.h"
 #include "sw_internal.h"
 
@@ -28,37 +30,45 @@
 
 SW_KERNELS_BEGIN
 
-// ---- correctly rounded scalar operations, both precisions
-__device__ __forceinline__ double ad(double a, double b) { return __dadd_rn(a, b); }
-__device__ __forceinline__ float ad(float a, float b) { return __fadd_rn(a, b); }
-__device__ __forceinline__ double sb(double a, double b) { return __dsub_rn(a, b); }
-__device__ __forceinline__ float sb(float a, float b) { return __fsub_rn(a, b); }
-__device__ __forceinline__ double ml(double a, double b) { return __dmul_rn(a, b); }
-__device__ __forceinline__ float ml(float a, float b) { return __fmul_rn(a, b); }
-__device__ __forceinline__ double dv(double a, double b) { return __ddiv_rn(a, b); }
-__device__ __forceinline__ float dv(float a, float b) { return __fdiv_rn(a, b); }
-__device__ __forceinline__ double sq(double a) { return __dsqrt_rn(a); }
-__device__ __forceinline__ float sq(float a) { return __fsqrt_rn(a); }
-__device__ __forceinline__ double mn(double a, double b) { return fmin(a, b); }
-__device__ __forceinline__ float mn(float a, float b) { return fminf(a, b); }
-__device__ __forceinline__ double ab(double a) { return fabs(a); }
-__device__ __forceinline__ float ab(float a) { return fabsf(a); }
+// ---- correctly rounded scalar operations, both precisions.  Host builds of
+// these functions (the host tile of the hybrid variant, csrc/host_tile.cu) use
+// the IEEE operation itself; that translation unit is compiled with
+// -ffp-contract=off, so nothing is fused there either.
+#ifdef __CUDA_ARCH__
+#define SW_OP(dev, host) dev
+#else
+#define SW_OP(dev, host) host
+#endif
+SW_HD double ad(double a, double b) { return SW_OP(__dadd_rn(a, b), a + b); }
+SW_HD float ad(float a, float b) { return SW_OP(__fadd_rn(a, b), a + b); }
+SW_HD double sb(double a, double b) { return SW_OP(__dsub_rn(a, b), a - b); }
+SW_HD float sb(float a, float b) { return SW_OP(__fsub_rn(a, b), a - b); }
+SW_HD double ml(double a, double b) { return SW_OP(__dmul_rn(a, b), a * b); }
+SW_HD float ml(float a, float b) { return SW_OP(__fmul_rn(a, b), a * b); }
+SW_HD double dv(double a, double b) { return SW_OP(__ddiv_rn(a, b), a / b); }
+SW_HD float dv(float a, float b) { return SW_OP(__fdiv_rn(a, b), a / b); }
+SW_HD double sq(double a) { return SW_OP(__dsqrt_rn(a), ::sqrt(a)); }
+SW_HD float sq(float a) { return SW_OP(__fsqrt_rn(a), ::sqrtf(a)); }
+SW_HD double mn(double a, double b) { return ::fmin(a, b); }
+SW_HD float mn(float a, float b) { return ::fminf(a, b); }
+SW_HD double ab(double a) { return ::fabs(a); }
+SW_HD float ab(float a) { return ::fabsf(a); }
 
-__device__ __forceinline__ double fm(double a, double b, double c) { return __fma_rn(a, b, c); }
-__device__ __forceinline__ float fm(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+SW_HD double fm(double a, double b, double c) { return SW_OP(__fma_rn(a, b, c), ::fma(a, b, c)); }
+SW_HD float fm(float a, float b, float c) { return SW_OP(__fmaf_rn(a, b, c), ::fmaf(a, b, c)); }
 
 // Products whose FP64 form runs on the integer pipe (exact_int.h), with the
 // bits of the FP64 multiply: 6 * c, and x * f with f = 2^k.  FP32 keeps its
 // multiply: the FP32 kernels are bound by instruction issue, not by a pipe.
-__device__ __forceinline__ double ml6(double c) { return mul6(c); }
-__device__ __forceinline__ float ml6(float c) { return ml(6.0f, c); }
-__device__ __forceinline__ double mlp2(double x, double f, int k) { return mul_pow2(x, f, k); }
-__device__ __forceinline__ float mlp2(float x, float f, int) { return ml(x, f); }
+SW_HD double ml6(double c) { return mul6(c); }
+SW_HD float ml6(float c) { return ml(6.0f, c); }
+SW_HD double mlp2(double x, double f, int k) { return mul_pow2(x, f, k); }
+SW_HD float mlp2(float x, float f, int) { return ml(x, f); }
 
 // ---------------------------------------------------------------- Heat
 // execFunc, Heat1D_SweptShared.cu:121-130: fourier*(T[l] + T[r]) + fourierTwo*T[c]
 template <typename T>
-__device__ __forceinline__ T heat_step(const Params<T> &p, T l, T c, T r) {
+SW_HD T heat_step(const Params<T> &p, T l, T c, T r) {
     return ad(ml(p.fo, ad(l, r)), ml(p.fo2, c));
 }
 
@@ -78,7 +88,7 @@ __device__ __forceinline__ T heat_step(const Params<T> &p, T l, T c, T r) {
 // (ml6) and, under KS_POW2, sec * d2 (mlp2, d2 = 2^d2_e): 12 FP64-pipe
 // operations per sub-step where the cell's square is supplied.
 template <typename T>
-__device__ __forceinline__ T ks_rhs_sq(const Params<T> &p, T ll, T l, T c, T r, T rr, T l2, T r2) {
+SW_HD T ks_rhs_sq(const Params<T> &p, T ll, T l, T c, T r, T rr, T l2, T r2) {
     const T conv = sb(r2, l2);  // l2 = l*l, r2 = r*r
     const T sec = fm(T(-2), c, ad(l, r));                        // (l + r) - 2c
     const T fourth = ad(fm(T(-4), r, ad(fm(T(-4), l, ll), ml6(c))), rr);  // ((ll - 4l) + 6c) - 4r + rr
@@ -90,28 +100,28 @@ __device__ __forceinline__ T ks_rhs_sq(const Params<T> &p, T ll, T l, T c, T r, 
 #endif
 }
 template <typename T>
-__device__ __forceinline__ T ks_rhs(const Params<T> &p, T ll, T l, T c, T r, T rr) {
+SW_HD T ks_rhs(const Params<T> &p, T ll, T l, T c, T r, T rr) {
     return ks_rhs_sq(p, ll, l, c, r, rr, ml(l, l), ml(r, r));
 }
 // stutterStep, KS1D_SweptShared.cu:159-164: u - dt/2 * rhs
 template <typename T>
-__device__ __forceinline__ T ks_predict(const Params<T> &p, T ll, T l, T c, T r, T rr) {
+SW_HD T ks_predict(const Params<T> &p, T ll, T l, T c, T r, T rr) {
     return sb(c, ml(p.dth, ks_rhs(p, ll, l, c, r, rr)));
 }
 // finalStep, KS1D_SweptShared.cu:166-171 added to u (classicKS :201-202): u + (-dt * rhs)
 template <typename T>
-__device__ __forceinline__ T ks_correct(const Params<T> &p, T u, T ll, T l, T c, T r, T rr) {
+SW_HD T ks_correct(const Params<T> &p, T u, T ll, T l, T c, T r, T rr) {
     return ad(u, ml(-p.dt, ks_rhs(p, ll, l, c, r, rr)));
 }
 // The same with the squares l*l and r*r of the neighbours supplied (each cell's
 // square is then formed once, by the thread that produced the value, instead
 // of by both of its neighbours; the product is the same __dmul_rn either way).
 template <typename T>
-__device__ __forceinline__ T ks_predict_sq(const Params<T> &p, T ll, T l, T c, T r, T rr, T l2, T r2) {
+SW_HD T ks_predict_sq(const Params<T> &p, T ll, T l, T c, T r, T rr, T l2, T r2) {
     return sb(c, ml(p.dth, ks_rhs_sq(p, ll, l, c, r, rr, l2, r2)));
 }
 template <typename T>
-__device__ __forceinline__ T ks_correct_sq(const Params<T> &p, T u, T ll, T l, T c, T r, T rr, T l2, T r2) {
+SW_HD T ks_correct_sq(const Params<T> &p, T u, T ll, T l, T c, T r, T rr, T l2, T r2) {
     return ad(u, ml(-p.dt, ks_rhs_sq(p, ll, l, c, r, rr, l2, r2)));
 }
 
@@ -138,34 +148,34 @@ struct Q3 {
     T x, y, z;
 };
 template <typename T>
-__device__ __forceinline__ Q3<T> q3(T x, T y, T z) { return Q3<T>{x, y, z}; }
+SW_HD Q3<T> q3(T x, T y, T z) { return Q3<T>{x, y, z}; }
 template <typename T>
-__device__ __forceinline__ Q3<T> qadd(Q3<T> a, Q3<T> b) { return q3(ad(a.x, b.x), ad(a.y, b.y), ad(a.z, b.z)); }
+SW_HD Q3<T> qadd(Q3<T> a, Q3<T> b) { return q3(ad(a.x, b.x), ad(a.y, b.y), ad(a.z, b.z)); }
 template <typename T>
-__device__ __forceinline__ Q3<T> qsub(Q3<T> a, Q3<T> b) { return q3(sb(a.x, b.x), sb(a.y, b.y), sb(a.z, b.z)); }
+SW_HD Q3<T> qsub(Q3<T> a, Q3<T> b) { return q3(sb(a.x, b.x), sb(a.y, b.y), sb(a.z, b.z)); }
 template <typename T>
-__device__ __forceinline__ Q3<T> qscale(T s, Q3<T> a) { return q3(ml(s, a.x), ml(s, a.y), ml(s, a.z)); }
+SW_HD Q3<T> qscale(T s, Q3<T> a) { return q3(ml(s, a.x), ml(s, a.y), ml(s, a.z)); }
 
 // pressure, Euler1D_SweptShared.cu:183-193: mgam*(E - (0.5*m*m/rho))
 // (The products by 0.5 and 2 below are exact scalings: mlp2 forms them on the
 // integer pipe in FP64, with the multiply's bits.)
 template <typename T>
-__device__ __forceinline__ T eu_pressure(const Params<T> &p, Q3<T> q) {
+SW_HD T eu_pressure(const Params<T> &p, Q3<T> q) {
     return ml(p.mgam, sb(q.z, dv(ml(mlp2(q.y, T(0.5), -1), q.y), q.x)));
 }
 // pressureHalf, :202-212: mgam*(z - 0.5*y*y)
 template <typename T>
-__device__ __forceinline__ T eu_pressure_half(const Params<T> &p, Q3<T> q) {
+SW_HD T eu_pressure_half(const Params<T> &p, Q3<T> q) {
     return ml(p.mgam, sb(q.z, ml(mlp2(q.y, T(0.5), -1), q.y)));
 }
 // limitor, :222-228: cur + 0.5*min(ratio,1)*(oth - cur)
 template <typename T>
-__device__ __forceinline__ Q3<T> eu_limit(Q3<T> cur, Q3<T> oth, T ratio) {
+SW_HD Q3<T> eu_limit(Q3<T> cur, Q3<T> oth, T ratio) {
     return qadd(cur, qscale(mlp2(mn(ratio, T(1)), T(0.5), -1), qsub(oth, cur)));
 }
 // eulerFlux, :237-257
 template <typename T>
-__device__ __forceinline__ Q3<T> eu_flux(const Params<T> &p, Q3<T> L, Q3<T> R) {
+SW_HD Q3<T> eu_flux(const Params<T> &p, Q3<T> L, Q3<T> R) {
     T uL = dv(L.y, L.x);
     T uR = dv(R.y, R.x);
     T pL = eu_pressure(p, L);
@@ -178,7 +188,7 @@ __device__ __forceinline__ Q3<T> eu_flux(const Params<T> &p, Q3<T> L, Q3<T> R) {
 }
 // eulerSpectral, :266-292
 template <typename T>
-__device__ __forceinline__ Q3<T> eu_spectral(const Params<T> &p, Q3<T> L, Q3<T> R) {
+SW_HD Q3<T> eu_spectral(const Params<T> &p, Q3<T> L, Q3<T> R) {
     T rl = sq(L.x), rr = sq(R.x);
     Q3<T> h;
     h.x = ml(rl, rr);
@@ -191,7 +201,7 @@ __device__ __forceinline__ Q3<T> eu_spectral(const Params<T> &p, Q3<T> L, Q3<T> 
 // The flux sum shared by eulerStutterStep / eulerFinalStep (:308-341, :354-380),
 // on five cells s[0..4] around s[2].
 template <typename T>
-__device__ __forceinline__ Q3<T> eu_flux_sum(const Params<T> &p, const Q3<T> (&s)[5], bool fl, bool fr) {
+SW_HD Q3<T> eu_flux_sum(const Params<T> &p, const Q3<T> (&s)[5], bool fl, bool fr) {
     const T Z = T(0);
     // Written as in the reference: P1-P0 = 2*s1.x*s0.x*(s1.z - s0.z) + (s0.y*s0.y*s1.x - s1.y*s1.y*s0.x)
     T pLL = fl ? Z : ad(ml(ml(mlp2(s[1].x, T(2), 1), s[0].x), sb(s[1].z, s[0].z)),
@@ -231,11 +241,11 @@ __device__ __forceinline__ Q3<T> eu_flux_sum(const Params<T> &p, const Q3<T> (&s
 //  * eu_combine: the cell's sum ((F_left + S_left) - F_right) - S_right, in
 //    the reference's order.
 template <typename T>
-__device__ __forceinline__ T eu_pdiff(Q3<T> a, Q3<T> b) {
+SW_HD T eu_pdiff(Q3<T> a, Q3<T> b) {
     return ad(ml(ml(mlp2(b.x, T(2), 1), a.x), sb(b.z, a.z)), sb(ml(ml(a.y, a.y), b.x), ml(ml(b.y, b.y), a.x)));
 }
 template <typename T>
-__device__ __forceinline__ void eu_iface(const Params<T> &p, Q3<T> am, Q3<T> a, Q3<T> b, Q3<T> bp, T Da, T Db, T Dbp,
+SW_HD void eu_iface(const Params<T> &p, Q3<T> am, Q3<T> a, Q3<T> b, Q3<T> bp, T Da, T Db, T Dbp,
                                          Q3<T> &F, Q3<T> &S) {
     const T Z = T(0);
     const bool skipA = (Da == Z) || (Db == Z) || ((Da < Z) != (Db < Z));
@@ -246,19 +256,19 @@ __device__ __forceinline__ void eu_iface(const Params<T> &p, Q3<T> am, Q3<T> a, 
     S = eu_spectral(p, tL, tR);
 }
 template <typename T>
-__device__ __forceinline__ Q3<T> eu_combine(Q3<T> Fl, Q3<T> Sl, Q3<T> Fr, Q3<T> Sr) {
+SW_HD Q3<T> eu_combine(Q3<T> Fl, Q3<T> Sl, Q3<T> Fr, Q3<T> Sr) {
     return qsub(qsub(qadd(Fl, Sl), Fr), Sr);
 }
 
 // eulerStutterStep result, :345: s2 + (0.25*dt_dx)*flux
 template <typename T>
-__device__ __forceinline__ Q3<T> eu_predict(const Params<T> &p, const Q3<T> (&s)[5], bool fl, bool fr) {
+SW_HD Q3<T> eu_predict(const Params<T> &p, const Q3<T> (&s)[5], bool fl, bool fr) {
     Q3<T> f = eu_flux_sum(p, s, fl, fr);
     return qadd(s[2], qscale(ml(T(0.25), p.dtdx), f));
 }
 // eulerFinalStep result added to the cell, :384 and classicEuler :420
 template <typename T>
-__device__ __forceinline__ Q3<T> eu_correct(const Params<T> &p, Q3<T> u, const Q3<T> (&s)[5], bool fl, bool fr) {
+SW_HD Q3<T> eu_correct(const Params<T> &p, Q3<T> u, const Q3<T> (&s)[5], bool fl, bool fr) {
     Q3<T> f = eu_flux_sum(p, s, fl, fr);
     return qadd(u, qscale(ml(T(0.5), p.dtdx), f));
 }

@@ -83,6 +83,13 @@ struct Ops {
                                     int *status, int W, int threads, int64_t n_diamonds, cudaStream_t s);
 };
 
+// The hybrid variant's host tile (host_tile.cu): the wrapping phase-1 tile of
+// a domain computed on the CPU from its two slots (sl: the last half-tile's,
+// sr: the first's); MODE_DIAMOND writes the slots back, MODE_DOWN the state's
+// first and last half-tiles.  params: a Params<float or double>.
+int host_tile_run(int problem, int prec, const void *params, int mode, void *sl, void *sr, void *state_first,
+                  void *state_last, int W);
+
 const Ops *heat_ops(int prec);
 const Ops *ks_ops(int prec);
 const Ops *ks_divide_ops(int prec);  // SW_FLAG_KS_DIVIDE (k_ks_div.cu)

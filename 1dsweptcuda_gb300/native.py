@@ -19,6 +19,7 @@ ALG_CLASSIC, ALG_SWEPT, ALG_VARIANT, ALG_SELFTEST = 0, 1, 2, 3
 BC_DEFAULT, BC_MIRROR, BC_PERIODIC, BC_DIRICHLET = 0, 1, 2, 3
 TIME_REFERENCE, TIME_STEPS = 0, 1
 FLAG_KS_DIVIDE = 1  # sw_config.flags: KS divides by 4dx, dx^2, dx^4 (the reference's DIVISE build)
+FLAG_HOST_TILE = 2  # sw_config.flags: the hybrid variant, each phase-1 pass's wrapping tile on the host
 COMPONENTS = {HEAT: 1, KS: 1, EULER: 3}
 PROBLEM_NAMES = {HEAT: "Heat", KS: "KS", EULER: "Euler"}
 

@@ -78,7 +78,16 @@ enum sw_flag {
      * reciprocals -- the reference's DIVISE build (KS1D_SweptShared.cu:111-132,
      * 904-914), kept for its divide-vs-multiply timing study.  At a power-of-two
      * dx (the reference's 0.5) both forms give the same bits. */
-    SW_FLAG_KS_DIVIDE = 1
+    SW_FLAG_KS_DIVIDE = 1,
+    /* The hybrid variant (the reference's alg 2 for Heat and Euler,
+     * Heat1D_SweptShared.cu:410-468,550-644; Euler1D_SweptShared.cu:761-835,
+     * 935-1050): in every phase-1 pass the tile that straddles the domain's
+     * ends is computed on the host CPU while the GPU computes the others; its
+     * two slots go down and back by copies on the run's stream.  Same results
+     * bit for bit.  With alg 1 (any problem) or alg 2 (Heat, Euler; then run as
+     * alg 1 with the host tile, as the reference's alg 2 is); not with
+     * SW_FLAG_KS_DIVIDE.  The sw_run / sw_run_device runs only. */
+    SW_FLAG_HOST_TILE = 2
 };
 
 /* ------------------------------------------------------------ run config */

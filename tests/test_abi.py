@@ -73,7 +73,7 @@ def test_enum_values_match_header(sw, tmp_path):
              "SW_BC_DEFAULT": native.BC_DEFAULT, "SW_BC_MIRROR": native.BC_MIRROR,
              "SW_BC_PERIODIC": native.BC_PERIODIC, "SW_BC_DIRICHLET": native.BC_DIRICHLET,
              "SW_TIME_REFERENCE": native.TIME_REFERENCE, "SW_TIME_STEPS": native.TIME_STEPS,
-             "SW_FLAG_KS_DIVIDE": native.FLAG_KS_DIVIDE}
+             "SW_FLAG_KS_DIVIDE": native.FLAG_KS_DIVIDE, "SW_FLAG_HOST_TILE": native.FLAG_HOST_TILE}
     src = tmp_path / "e.c"
     src.write_text("\n".join(['#include <stdio.h>', '#include "swept1d.h"', "int main(void){"] +
                               ['printf("%s %%d\\n", (int)%s);' % (n, n) for n in names] + ["return 0;}"]))
@@ -190,3 +190,16 @@ def test_ensemble_generator():
     assert max(abs(float(p.mean())) for p in parts[:50]) < 1e-9
     nx2, u2 = ens.make_ensemble(n_domains=4096)
     assert (nx2 == nx).all() and np.array_equal(u2, u)   # seeded
+
+
+def test_host_tile_flag_rules(sw):
+    """SW_FLAG_HOST_TILE: alg 1 for any problem, alg 2 for Heat and Euler (the
+    reference's hybrid), never with the dividing KS build or classic."""
+    ok = [(0, 1), (0, 2), (2, 1), (2, 2), (1, 1)]
+    bad = [(1, 2), (0, 0), (1, 0)]
+    for problem, alg in ok + bad:
+        dt = 1e-5 if problem == 2 else 1e-3
+        cfg = sw.make_config(problem, 8, alg=alg, nx=1024, tpb=64, dt=dt, flags=sw.FLAG_HOST_TILE)
+        assert (sw.validate(cfg) == 0) == ((problem, alg) in ok), (problem, alg)
+    ks = sw.make_config(1, 8, alg=1, nx=1024, tpb=64, dt=1e-3, flags=sw.FLAG_HOST_TILE | sw.FLAG_KS_DIVIDE)
+    assert sw.validate(ks) == -1

@@ -24,7 +24,7 @@ def test_flag_checks(sw):
     assert sw.validate(sw.make_config(KS, 8, flags=sw.FLAG_KS_DIVIDE)) == 0
     for problem in (HEAT, EULER):
         assert sw.validate(sw.make_config(problem, 8, flags=sw.FLAG_KS_DIVIDE)) == -1  # SW_ERR_ARG
-    assert sw.validate(sw.make_config(KS, 8, flags=2)) == -1
+    assert sw.validate(sw.make_config(KS, 8, flags=4)) == -1   # no such flag
 
 
 @pytest.mark.parametrize("prec", [8, 4])
