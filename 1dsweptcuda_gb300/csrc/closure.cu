@@ -41,7 +41,7 @@ constexpr int NZ2 = 144;        // 9 m-tiles of 16 rows
 constexpr int NA2 = TOUT + 4;   // 132 a2 rows used
 constexpr int LDB = 40;         // bf16 row stride (80 B: conflict-free fragment reads)
 constexpr int LDF = 33;         // fp32 row stride
-constexpr int THREADS = 256;
+constexpr int THREADS = 256;  // (9 warps, one per layer-2 m-tile, measured slower: 106.5 against 102.3 us per step)
 // parameter offsets (flat FP32 vector); the last value is the output scale s
 // (delta = s * net(u)), fixed by the caller and left alone by training
 constexpr int OW1 = 0, OB1 = 160, OW2 = 192, OB2 = 5312, OW3 = 5344, OB3 = 5504, OSCALE = 5505;
@@ -59,9 +59,20 @@ __device__ __forceinline__ float tanh_sfu(float x) {
     asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
     return y;
 }
-__device__ __forceinline__ float gelu(float x) {
-    const float t = tanh_sfu(kGeluC * x * fmaf(kGeluA * x, x, 1.0f));
-    return 0.5f * x * (1.0f + t);
+__device__ __forceinline__ float gelu(float x) {  // x/2 + (x/2) t, the operations of gelu2 below
+    const float t = tanh_sfu((kGeluC * x) * fmaf(kGeluA, x * x, 1.0f));
+    const float hx = 0.5f * x;
+    return fmaf(hx, t, hx);
+}
+// Two GELUs with paired FP32 instructions (one f32x2 instruction does the
+// arithmetic of two lanes' worth: the forward step is bound by instruction
+// issue).  Each component is gelu of that component, operation for operation.
+__device__ __forceinline__ float2 f2(float v) { return make_float2(v, v); }
+__device__ __forceinline__ float2 gelu2(float2 x) {
+    const float2 inner = __ffma2_rn(f2(kGeluA), __fmul2_rn(x, x), f2(1.0f));
+    const float2 arg = __fmul2_rn(__fmul2_rn(f2(kGeluC), x), inner);
+    const float2 hx = __fmul2_rn(f2(0.5f), x);
+    return __ffma2_rn(hx, make_float2(tanh_sfu(arg.x), tanh_sfu(arg.y)), hx);
 }
 __device__ __forceinline__ float gelu_grad(float x) {
     const float x2 = x * x;
@@ -165,11 +176,32 @@ __device__ void forward_12(Smem &s) {
 #pragma unroll
         for (int t = 0; t < KW; ++t) w[t] = s.w1[o * KW + t];
         const float b = s.b1[o];
-        if (r0 < r1) {
+        int r = r0;
+        if constexpr (!TRAIN) {
+            // two rows per iteration as f32x2 pairs: window v[0..5] = inputs r .. r+5
+            float v[KW + 1];
+            if (r0 < r1) {
 #pragma unroll
-            for (int t = 0; t < KW - 1; ++t) u[t + 1] = s.us[r0 + t];
+                for (int t = 0; t < KW - 1; ++t) v[t + 2] = s.us[r0 + t];
+            }
+            for (; r + 1 < r1; r += 2) {
+#pragma unroll
+                for (int t = 0; t < KW - 1; ++t) v[t] = v[t + 2];
+                v[KW - 1] = s.us[r + KW - 1];
+                v[KW] = s.us[r + KW];
+                float2 z = f2(b);
+#pragma unroll
+                for (int t = 0; t < KW; ++t) z = __ffma2_rn(f2(w[t]), make_float2(v[t], v[t + 1]), z);
+                const float2 g = gelu2(z);
+                s.a1[r * LDB + o] = __float2bfloat16_rn(g.x);
+                s.a1[(r + 1) * LDB + o] = __float2bfloat16_rn(g.y);
+            }
         }
-        for (int r = r0; r < r1; ++r) {
+        if (r < r1) {
+#pragma unroll
+            for (int t = 0; t < KW - 1; ++t) u[t + 1] = s.us[r + t];
+        }
+        for (; r < r1; ++r) {
 #pragma unroll
             for (int t = 0; t < KW - 1; ++t) u[t] = u[t + 1];
             u[KW - 1] = s.us[r + KW - 1];
@@ -223,29 +255,35 @@ __device__ void forward_12(Smem &s) {
                 }
             }
         } else {
-            float p[2][KW] = {};
+            // GELU on channel pairs (o, o+1) of a row, the tap sums on row pairs (r0, r1)
+            float2 pr[KW];
+#pragma unroll
+            for (int t = 0; t < KW; ++t) pr[t] = f2(0.0f);
 #pragma unroll
             for (int nt = 0; nt < 4; ++nt) {
+                const int o = nt * 8 + 2 * q;
+                const float2 bias = make_float2(s.b2[o], s.b2[o + 1]);
+                const float2 g0 = gelu2(__fadd2_rn(make_float2(acc[nt][0], acc[nt][1]), bias));  // row r0
+                const float2 g1 = gelu2(__fadd2_rn(make_float2(acc[nt][2], acc[nt][3]), bias));  // row r1
+                const float2 c0 = make_float2(g0.x, g1.x), c1 = make_float2(g0.y, g1.y);         // channel o, o+1
 #pragma unroll
-                for (int e = 0; e < 4; ++e) {
-                    const int o = nt * 8 + 2 * q + (e & 1);
-                    const float a = gelu(acc[nt][e] + s.b2[o]);
-#pragma unroll
-                    for (int t = 0; t < KW; ++t) p[e >> 1][t] = fmaf(s.w3[o * KW + t], a, p[e >> 1][t]);
+                for (int t = 0; t < KW; ++t) {
+                    pr[t] = __ffma2_rn(f2(s.w3[o * KW + t]), c0, pr[t]);
+                    pr[t] = __ffma2_rn(f2(s.w3[(o + 1) * KW + t]), c1, pr[t]);
                 }
             }
 #pragma unroll
-            for (int h = 0; h < 2; ++h)
-#pragma unroll
-                for (int t = 0; t < KW; ++t) {
-                    p[h][t] += __shfl_xor_sync(0xffffffffu, p[h][t], 1);
-                    p[h][t] += __shfl_xor_sync(0xffffffffu, p[h][t], 2);
-                }
+            for (int t = 0; t < KW; ++t) {
+                pr[t].x += __shfl_xor_sync(0xffffffffu, pr[t].x, 1);
+                pr[t].y += __shfl_xor_sync(0xffffffffu, pr[t].y, 1);
+                pr[t].x += __shfl_xor_sync(0xffffffffu, pr[t].x, 2);
+                pr[t].y += __shfl_xor_sync(0xffffffffu, pr[t].y, 2);
+            }
             if (q == 0) {
 #pragma unroll
                 for (int t = 0; t < KW; ++t) {
-                    if (r0 < NA2) s.p3[t * NA2 + r0] = p[0][t];
-                    if (r1 < NA2) s.p3[t * NA2 + r1] = p[1][t];
+                    if (r0 < NA2) s.p3[t * NA2 + r0] = pr[t].x;
+                    if (r1 < NA2) s.p3[t * NA2 + r1] = pr[t].y;
                 }
             }
         }
