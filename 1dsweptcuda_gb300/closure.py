@@ -216,74 +216,42 @@ def run_adaptive(solver, closure: Closure, fine0, coarse_steps: int, segment: in
     passes tau, the run stops and every domain is solved by the fine solver
     from fine0 in one batch, so the answer is the fine solution itself.
 
+    The loop runs inside the library (sw_closure_adaptive), one call for the
+    whole run, so a segment costs its kernels and a few small copies rather
+    than a host round trip per tensor operation.
+
     Returns (u, info): u (n_dom, 1024) FP32 at t0 + coarse_steps * 0.02, and
     the segments run with the closure and plain, whether it fell back, the
     sample's final error (max and mean) and a per-segment log."""
     torch = _torch()
+    sw = _sw()
     own_judge = judge is None or judge is solver   # the judge keeps graphs of its own shape
     if own_judge:
-        judge = _sw().Solver(solver.device)
-    u = coarse_grain(solver, fine0)
-    n_dom = u.shape[0]
-    idx = shadow_domains(n_dom, shadow_every, seed)
-    # the shadow lives in a buffer kept with the judge: the fine solver's captured graph is
-    # tied to its state's address, so the same buffer lets later calls replay that graph
-    shadow = getattr(judge, "_shadow_buf", None)
-    if shadow is None or shadow.shape != (int(idx.numel()), fine0.shape[1]):
-        shadow = torch.empty((int(idx.numel()), fine0.shape[1]), dtype=fine0.dtype, device=fine0.device)
-        judge._shadow_buf = shadow
-    shadow.copy_(fine0[idx])   # (the judge's runs order after the legacy default stream: no wait needed)
-    info = {"closure": 0, "plain": 0, "fallback": False, "shadow_domains": int(idx.numel()), "log": []}
-    on = {"plain": False, "closure": True}
-
-    def err_of(v, ref):
-        return (v.double() - ref.double()).norm(dim=1) / ref.double().norm(dim=1)
-
-    done, prev, pick = 0, 0.0, None
-    while done < coarse_steps:
-        k = min(segment, coarse_steps - done)
-        # the judge's segment first: its few launches run alone on the GPU (run beside the
-        # ensemble's thousands of blocks, each of them waited for an SM slot)
-        advance_fine(judge, shadow, k * FACTOR)
-        ref = coarse_grain(judge, shadow)
-        if pick is None:  # first segment: both variants on the sample, then the ensemble with the better one
-            runs = {}
-            for name in on:
-                v = u[idx].contiguous()
-                closure.step(v, k, use_closure=on[name])
-                runs[name] = err_of(v, ref)
-            means = torch.stack([runs["plain"].mean(), runs["closure"].mean()]).tolist()
-            pick = "plain" if means[0] <= means[1] else "closure"
-            closure.step(u, k, use_closure=on[pick])
-            e_cur, e_alt = runs[pick], runs["plain" if pick == "closure" else "closure"]
-        else:
-            other = "plain" if pick == "closure" else "closure"
-            v = u[idx].contiguous()
-            closure.step(v, k, use_closure=on[other])
-            closure.step(u, k, use_closure=on[pick])
-            e_cur, e_alt = err_of(u[idx], ref), err_of(v, ref)
-        used = pick
-        # the certificate: the sample's mean relative L2 error (the metric's form); one readback
-        err, err_max, err_other = torch.stack([e_cur.mean(), e_cur.max(), e_alt.mean()]).tolist()
-        done += k
-        info["log"].append({"t": done * COARSE_DT, "used": used, "err": err, "err_max": err_max,
-                            "err_other": err_other})
-        left = (coarse_steps - done) / max(k, 1)   # segments still to run
-        if err > tau or err + max(err - prev, 0.0) * left > tau:
-            info["fallback"] = True
-            break
-        info[used] += 1
-        info["shadow_mean_rel_l2"], info["shadow_max_rel_l2"] = err, err_max
-        prev = err
-        if err_other < err:
-            pick = "plain" if used == "closure" else "closure"
+        judge = sw.Solver(solver.device)
+    n_dom = fine0.shape[0]
+    off = int(np.random.default_rng(seed).integers(shadow_every))
+    u = torch.empty((n_dom, COARSE_NX), dtype=torch.float32, device=fine0.device)
+    info = sw.native.AdaptiveInfo()
+    cap = coarse_steps // max(segment, 1) + 2
+    log = (C.c_double * (4 * cap))()
+    fine0 = fine0.contiguous()
+    rc = sw.library().sw_closure_adaptive(solver._ctx, judge._ctx, C.byref(closure.coarse_config()),
+                                          C.byref(fine_config(sw, 0)), closure.theta.data_ptr(), fine0.data_ptr(),
+                                          n_dom, FINE_NX, FACTOR, coarse_steps, segment, tau, shadow_every, off,
+                                          u.data_ptr(), C.byref(info), log, cap)
     if own_judge:
         judge.close()
-    if info["fallback"]:
-        f = fine0.clone()
-        advance_fine(solver, f, coarse_steps * FACTOR)
-        u = coarse_grain(solver, f)
-    return u, info
+    if rc:
+        raise solver._err(rc, "sw_closure_adaptive")
+    out = {"closure": info.closure_segments, "plain": info.plain_segments, "fallback": bool(info.fallback),
+           "shadow_domains": info.n_shadow, "log": []}
+    if info.closure_segments + info.plain_segments:
+        out["shadow_mean_rel_l2"], out["shadow_max_rel_l2"] = info.shadow_mean_rel_l2, info.shadow_max_rel_l2
+    for i in range(info.n_log):
+        steps, used, err, other = log[4 * i:4 * i + 4]
+        out["log"].append({"t": steps * COARSE_DT, "used": "closure" if used else "plain", "err": err,
+                           "err_other": other})
+    return u, out
 
 
 CHAOS_SPINUP = 12500   # coarse steps (t = 250): the ensemble's long waves have broken into KS chaos
@@ -413,9 +381,11 @@ def evaluate(n_train: int = 512, snapshots: int = 64, n_eval: int = 1024, ic_hor
 def bench_target(solver) -> dict:
     """The surrogate-corrected ensemble's line for the benchmark: the
     1024-domain, fine 4096 / coarse 1024 configuration, closure trained here on
-    512 fine trajectories x 64 snapshots of developed chaos (18000 Adam steps,
-    step-decayed rate), tau = 1e-3."""
-    out = evaluate(n_train=512, snapshots=64, n_eval=1024, train_steps=18000, decay=True, solver=solver)
+    2048 fine trajectories x 128 snapshots of developed chaos (30000 Adam
+    steps, step-decayed rate), tau = 1e-3; horizons 10, 30, 40 from the IC and
+    0.1 .. 0.4 from developed chaos."""
+    out = evaluate(n_train=2048, snapshots=128, n_eval=1024, ic_horizons=(10.0, 30.0, 40.0),
+                   chaos_horizons=(0.1, 0.2, 0.3, 0.4), train_steps=30000, decay=True, solver=solver)
     out["note"] = ("time-to-tf at mean rel-L2 <= 1e-3 against the coarse-grained fine FP64 solution; "
                    "tf = 200 lies beyond KS's predictability horizon for any coarse scheme (errors grow e-fold "
                    "every ~4 time units in developed chaos), so the adaptive run falls back to the fine solver there")

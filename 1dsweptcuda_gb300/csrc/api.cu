@@ -490,7 +490,7 @@ int sw_ctx_destroy(sw_ctx *c) {
     if (!c) return SW_ERR_ARG;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
-    void *bufs[] = {c->d_state, c->d_work, c->d_slots, c->d_io, c->d_flags, c->d_status, c->d_w2p};
+    void *bufs[] = {c->d_state, c->d_work, c->d_slots, c->d_io, c->d_flags, c->d_status, c->d_w2p, c->d_judge};
     for (void *b : bufs)
         if (b) cudaFree(b);
     if (c->h_pin) cudaFreeHost(c->h_pin);

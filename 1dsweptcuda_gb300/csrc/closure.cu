@@ -542,6 +542,41 @@ __global__ void k_coarse_grain(const double *__restrict__ fine, float *__restric
     coarse[j] = (float)(a / factor);
 }
 
+// Rows idx[0..m) of the (domains x n) array src into the (m x n) array dst.
+template <typename T>
+__global__ void k_gather_rows(const T *__restrict__ src, const int32_t *__restrict__ idx, int64_t n,
+                              T *__restrict__ dst) {
+    const T *a = src + (int64_t)idx[blockIdx.x] * n;
+    T *b = dst + (int64_t)blockIdx.x * n;
+    for (int64_t j = threadIdx.x; j < n; j += blockDim.x) b[j] = a[j];
+}
+
+// out[d] = ||a_d - b_d|| / ||b_d|| (FP64 sums) for the m rows of b; a's row d is
+// row rows[d] of a when rows is given, else row d.  One block per row.
+__global__ void __launch_bounds__(256) k_rel_l2(const float *__restrict__ a, const int32_t *__restrict__ rows,
+                                                const float *__restrict__ b, int64_t n, double *__restrict__ out) {
+    const float *x = a + (int64_t)(rows ? rows[blockIdx.x] : (int)blockIdx.x) * n;
+    const float *y = b + (int64_t)blockIdx.x * n;
+    double s1 = 0.0, s2 = 0.0;
+    for (int64_t j = threadIdx.x; j < n; j += blockDim.x) {
+        const double d = (double)x[j] - (double)y[j];
+        s1 += d * d;
+        s2 += (double)y[j] * (double)y[j];
+    }
+    __shared__ double r1[256], r2[256];
+    r1[threadIdx.x] = s1;
+    r2[threadIdx.x] = s2;
+    __syncthreads();
+    for (int k = blockDim.x / 2; k > 0; k >>= 1) {
+        if ((int)threadIdx.x < k) {
+            r1[threadIdx.x] += r1[threadIdx.x + k];
+            r2[threadIdx.x] += r2[threadIdx.x + k];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[blockIdx.x] = sqrt(r1[0] / r2[0]);
+}
+
 constexpr size_t smem_bytes() { return sizeof(Smem); }
 constexpr size_t smem_fwd_bytes() { return offsetof(Smem, a2); }
 
@@ -740,6 +775,137 @@ int sw_closure_train(sw_ctx *ctx, float *theta, const float *inputs, const float
     cudaFree(rows);
     cudaFree(buf);
     return rc;
+}
+
+int sw_closure_adaptive(sw_ctx *ctx, sw_ctx *judge, const sw_config *coarse, const sw_config *fine,
+                        const float *theta, const double *fine0, int32_t n_dom, int64_t n_fine, int32_t factor,
+                        int64_t coarse_steps, int64_t segment, double tau, int32_t shadow_every,
+                        int32_t shadow_offset, float *u_out, sw_adaptive_info *info, double *log_out,
+                        int32_t log_cap) {
+    if (!ctx || !judge || judge == ctx || !coarse || !fine || !fine0 || !u_out || !info) return SW_ERR_ARG;
+    if (factor < 1 || n_fine % factor || shadow_every < 1 || shadow_offset < 0 || shadow_offset >= shadow_every ||
+        segment < 1 || coarse_steps < 0 || !(tau >= 0))
+        return SW_ERR_ARG;
+    if (judge->device != ctx->device) return fail(ctx, SW_ERR_ARG, "the judge context must be on the run's device");
+    const int64_t n = n_fine / factor;
+    int rc = closure_check(ctx, n_dom, n);
+    if (rc) return rc;
+    std::vector<int32_t> idx;
+    for (int32_t d = shadow_offset; d < n_dom; d += shadow_every) idx.push_back(d);
+    if (idx.empty()) return fail(ctx, SW_ERR_ARG, "the judge's sample is empty");
+    const int32_t m = (int32_t)idx.size();
+    SW_CUDA(ctx, cudaSetDevice(ctx->device));
+    // run context scratch: the sample's coarse rows and reference (m x n floats each), indices, errors
+    const size_t fb = sizeof(float) * (size_t)m * n;
+    SW_CUDA(ctx, grow_dev(&ctx->d_judge, &ctx->n_judge, 2 * fb + 4 * sizeof(double) * m + sizeof(int32_t) * m + 64));
+    float *samp = static_cast<float *>(ctx->d_judge), *ref = samp + (size_t)m * n;
+    double *err = reinterpret_cast<double *>(ref + (size_t)m * n);  // [2][m]
+    int32_t *idx_d = reinterpret_cast<int32_t *>(err + 2 * m);
+    SW_CUDA(ctx, grow_dev(&judge->d_judge, &judge->n_judge, sizeof(double) * (size_t)m * n_fine));
+    double *shadow = static_cast<double *>(judge->d_judge);
+    SW_CUDA(ctx, cudaMemcpy(idx_d, idx.data(), sizeof(int32_t) * m, cudaMemcpyHostToDevice));
+    if ((rc = after_legacy(ctx)) != SW_OK) return rc;
+    cudaStream_t s = ctx->stream;
+    cl::k_gather_rows<double><<<m, 256, 0, s>>>(fine0, idx_d, n_fine, shadow);
+    SW_CUDA(ctx, cudaGetLastError());
+    SW_CUDA(ctx, cudaStreamSynchronize(s));
+    if ((rc = sw_coarse_grain(ctx, fine0, u_out, (int64_t)n_dom * n, factor))) return rc;
+    std::memset(info, 0, sizeof(*info));
+    info->n_shadow = m;
+    std::vector<int64_t> nx_s((size_t)m, n_fine);
+    std::vector<double> h_err(2 * (size_t)m);
+    sw_config fc = *fine;
+    fc.time_mode = SW_TIME_STEPS;
+    auto rel = [&](const float *a, const int32_t *rows, int slot) -> int {
+        cl::k_rel_l2<<<m, 256, 0, s>>>(a, rows, ref, n, err + (size_t)slot * m);
+        SW_CUDA(ctx, cudaGetLastError());
+        return SW_OK;
+    };
+    auto stats = [&](int slot, double *mean, double *mx) {
+        double a = 0.0, b = 0.0;
+        for (int32_t d = 0; d < m; ++d) {
+            a += h_err[(size_t)slot * m + d];
+            b = std::max(b, h_err[(size_t)slot * m + d]);
+        }
+        *mean = a / m;
+        *mx = b;
+    };
+    int64_t done = 0;
+    int pick = -1;  // 0 plain, 1 closure
+    double prev = 0.0;
+    int32_t nlog = 0;
+    while (done < coarse_steps) {
+        const int64_t k = std::min(segment, coarse_steps - done);
+        // the judge's segment first: its few launches run alone on the GPU
+        fc.n_steps = k * factor;
+        if ((rc = sw_run_batch_device(judge, &fc, m, nx_s.data(), shadow, nullptr, nullptr))) return rc;
+        if ((rc = sw_coarse_grain(judge, shadow, ref, (int64_t)m * n, factor))) return rc;
+        int cur_slot, alt_slot;
+        if (pick < 0) {  // first segment: both variants on the sample, the better one on the ensemble
+            for (int v = 0; v < 2; ++v) {
+                cl::k_gather_rows<float><<<m, 256, 0, s>>>(u_out, idx_d, n, samp);
+                SW_CUDA(ctx, cudaGetLastError());
+                if ((rc = sw_closure_step(ctx, coarse, theta, samp, m, n, k, v, nullptr))) return rc;
+                if ((rc = rel(samp, nullptr, v))) return rc;
+            }
+            SW_CUDA(ctx, cudaMemcpyAsync(h_err.data(), err, sizeof(double) * 2 * m, cudaMemcpyDeviceToHost, s));
+            SW_CUDA(ctx, cudaStreamSynchronize(s));
+            double m0, m1, x0, x1;
+            stats(0, &m0, &x0);
+            stats(1, &m1, &x1);
+            pick = (m1 < m0) ? 1 : 0;
+            if ((rc = sw_closure_step(ctx, coarse, theta, u_out, n_dom, n, k, pick, nullptr))) return rc;
+            cur_slot = pick;
+            alt_slot = 1 - pick;
+        } else {  // the ensemble runs the pick, the other variant runs on the sample
+            cl::k_gather_rows<float><<<m, 256, 0, s>>>(u_out, idx_d, n, samp);
+            SW_CUDA(ctx, cudaGetLastError());
+            if ((rc = sw_closure_step(ctx, coarse, theta, samp, m, n, k, 1 - pick, nullptr))) return rc;
+            if ((rc = sw_closure_step(ctx, coarse, theta, u_out, n_dom, n, k, pick, nullptr))) return rc;
+            if ((rc = rel(u_out, idx_d, 0))) return rc;
+            if ((rc = rel(samp, nullptr, 1))) return rc;
+            SW_CUDA(ctx, cudaMemcpyAsync(h_err.data(), err, sizeof(double) * 2 * m, cudaMemcpyDeviceToHost, s));
+            SW_CUDA(ctx, cudaStreamSynchronize(s));
+            cur_slot = 0;
+            alt_slot = 1;
+        }
+        double e, emax, eo, eomax;
+        stats(cur_slot, &e, &emax);  // the certificate: the sample's mean relative L2 error
+        stats(alt_slot, &eo, &eomax);
+        done += k;
+        if (log_out && nlog < log_cap) {
+            double *row = log_out + 4 * (size_t)nlog;
+            row[0] = (double)done;
+            row[1] = pick;
+            row[2] = e;
+            row[3] = eo;
+            ++nlog;
+        }
+        const double left = (double)(coarse_steps - done) / (double)k;  // segments still to run
+        if (e > tau || e + std::max(e - prev, 0.0) * left > tau) {
+            info->fallback = 1;
+            break;
+        }
+        if (pick == 1) ++info->closure_segments;
+        else ++info->plain_segments;
+        info->shadow_mean_rel_l2 = e;
+        info->shadow_max_rel_l2 = emax;
+        prev = e;
+        if (eo < e) pick = 1 - pick;
+    }
+    info->n_log = nlog;
+    if (info->fallback) {  // every domain by the fine solver from fine0: the answer is the fine solution
+        const size_t bytes = sizeof(double) * (size_t)n_dom * n_fine;
+        SW_CUDA(ctx, grow_dev(&ctx->d_state, &ctx->n_state, bytes));
+        SW_CUDA(ctx, cudaMemcpyAsync(ctx->d_state, fine0, bytes, cudaMemcpyDeviceToDevice, s));
+        SW_CUDA(ctx, cudaStreamSynchronize(s));
+        std::vector<int64_t> nx_all((size_t)n_dom, n_fine);
+        fc.n_steps = coarse_steps * factor;
+        if ((rc = sw_run_batch_device(ctx, &fc, n_dom, nx_all.data(), ctx->d_state, nullptr, nullptr))) return rc;
+        if ((rc = sw_coarse_grain(ctx, static_cast<const double *>(ctx->d_state), u_out, (int64_t)n_dom * n, factor)))
+            return rc;
+    }
+    return SW_OK;
 }
 
 int sw_coarse_grain(sw_ctx *ctx, const double *fine, float *coarse, int64_t n_coarse_total, int32_t factor) {

@@ -112,6 +112,8 @@ struct sw_ctx {
     size_t n_flags = 0;
     int *d_status = nullptr;
     void *d_w2p = nullptr;  // closure layer-2 weights, BF16, in the kernels' shared-memory layout
+    void *d_judge = nullptr;  // sw_closure_adaptive: the sample's rows, errors (run context) or fine shadow (judge)
+    size_t n_judge = 0;
     void *h_pin = nullptr;
     size_t n_pin = 0;
     void *h_tile = nullptr;         // the hybrid variant's host tile: its two slots and two state pieces

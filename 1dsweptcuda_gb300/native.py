@@ -32,7 +32,7 @@ EXPORTED = ["sw_abi_version", "sw_strerror", "sw_ctx_create", "sw_ctx_destroy", 
             "sw_run_device", "sw_plan", "sw_cli_main", "sw_run_batch", "sw_run_batch_device",
             "sw_query_tuning", "sw_run_device_noalloc", "sw_closure_infer", "sw_closure_step",
             "sw_closure_grad", "sw_closure_adam", "sw_closure_train", "sw_coarse_grain", "sw_wait_probe",
-            "sw_fp64_rates", "sw_swept_pass"]
+            "sw_fp64_rates", "sw_swept_pass", "sw_closure_adaptive"]
 CLOSURE_PARAMS = 5506
 CUDA_STREAM_LEGACY = 1  # cudaStreamLegacy: the legacy default stream (a stream argument of 0 means the context's own)
 
@@ -75,6 +75,12 @@ class Result(C.Structure):
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class AdaptiveInfo(C.Structure):
+    _fields_ = [("closure_segments", C.c_int32), ("plain_segments", C.c_int32), ("fallback", C.c_int32),
+                ("n_shadow", C.c_int32), ("n_log", C.c_int32), ("shadow_mean_rel_l2", C.c_double),
+                ("shadow_max_rel_l2", C.c_double)]
 
 
 class PlanInfo(C.Structure):
@@ -149,11 +155,14 @@ def library():
     dp = C.POINTER(C.c_double)
     L.sw_fp64_rates.argtypes = [vp, dp, dp, dp]
     L.sw_swept_pass.argtypes = [vp, cp, C.c_int32, C.c_int32, vp, vp, vp]
+    L.sw_closure_adaptive.argtypes = [vp, vp, cp, cp, vp, vp, C.c_int32, C.c_int64, C.c_int32, C.c_int64, C.c_int64,
+                                      C.c_double, C.c_int32, C.c_int32, vp, C.POINTER(AdaptiveInfo),
+                                      C.POINTER(C.c_double), C.c_int32]
     for name in ("sw_ctx_create", "sw_ctx_destroy", "sw_config_init", "sw_validate", "sw_constants_of",
                  "sw_initial_condition", "sw_run", "sw_run_device", "sw_cli_main", "sw_plan", "sw_run_batch",
                  "sw_run_batch_device", "sw_query_tuning", "sw_run_device_noalloc", "sw_closure_infer",
                  "sw_closure_step", "sw_closure_grad", "sw_closure_adam", "sw_closure_train", "sw_coarse_grain",
-                 "sw_fp64_rates", "sw_swept_pass"):
+                 "sw_fp64_rates", "sw_swept_pass", "sw_closure_adaptive"):
         getattr(L, name).restype = C.c_int
     _lib = L
     return L

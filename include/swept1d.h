@@ -287,6 +287,38 @@ int sw_closure_adam(sw_ctx *ctx, float *theta, const float *grad, float *m, floa
  * `steps` floats) receives the loss of each step. */
 int sw_closure_train(sw_ctx *ctx, float *theta, const float *inputs, const float *targets, int64_t n_samples,
                      int64_t n, int32_t batch, int32_t steps, float lr, uint64_t seed, float *loss_host);
+/* The certified coarse run of an ensemble (no counterpart in the reference):
+ * n_dom domains of n_fine FP64 cells at t0 (fine0, device) are coarse-grained
+ * by `factor` into u_out (n_dom x n_fine/factor FP32, device) and advanced
+ * coarse_steps coarse steps (`coarse`: KS FP32; each coarse step is `factor`
+ * steps of `fine`, a KS FP64 swept config) segment by segment.  The judge is
+ * the fine solver on a second context, `judge`: it advances the exact fine
+ * state of the sample d = shadow_offset, shadow_offset + shadow_every, ...
+ * ahead of each segment.  In the first segment both the closure-corrected
+ * and the plain coarse step advance the sample and the one nearer the
+ * coarse-grained shadow (mean relative L2 error) advances the ensemble; after
+ * that the ensemble runs the pick while the other variant runs on the sample,
+ * and the pick switches when the other ends a segment nearer.  The sample's
+ * mean relative L2 error is the certificate: when it passes tau, or its last
+ * growth extrapolated linearly to the end passes tau, every domain is solved
+ * by the fine solver from fine0 instead (info->fallback = 1), so u_out is
+ * then the coarse-grained fine solution.  log_out (optional, host) receives
+ * up to log_cap rows of (coarse steps done, variant 0 plain / 1 closure,
+ * certificate, the other variant's error). */
+typedef struct sw_adaptive_info {
+    int32_t closure_segments;   /* segments the ensemble ran with the closure */
+    int32_t plain_segments;     /* segments it ran with the plain coarse step */
+    int32_t fallback;           /* 1: the fine solver's answer was returned */
+    int32_t n_shadow;           /* domains in the judge's sample */
+    int32_t n_log;              /* rows written to log_out */
+    double shadow_mean_rel_l2;  /* the last kept segment's certificate */
+    double shadow_max_rel_l2;   /* the sample's largest error then */
+} sw_adaptive_info;
+int sw_closure_adaptive(sw_ctx *ctx, sw_ctx *judge, const sw_config *coarse, const sw_config *fine,
+                        const float *theta, const double *fine0, int32_t n_dom, int64_t n_fine, int32_t factor,
+                        int64_t coarse_steps, int64_t segment, double tau, int32_t shadow_every,
+                        int32_t shadow_offset, float *u_out, sw_adaptive_info *info, double *log_out,
+                        int32_t log_cap);
 /* Cell averages of `factor` consecutive fine FP64 cells into FP32 coarse cells. */
 int sw_coarse_grain(sw_ctx *ctx, const double *fine, float *coarse, int64_t n_coarse_total, int32_t factor);
 

@@ -46,7 +46,7 @@ def test_struct_layouts_match_header(sw, tmp_path):
     native = import_module("1dsweptcuda_gb300.native")
     src = tmp_path / "l.c"
     fields = {"sw_config": native.Config, "sw_constants": native.Constants, "sw_result": native.Result,
-              "sw_plan_info": native.PlanInfo, "sw_tuning": native.Tuning}
+              "sw_plan_info": native.PlanInfo, "sw_tuning": native.Tuning, "sw_adaptive_info": native.AdaptiveInfo}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "swept1d.h"', "int main(void){"]
     for cname, py in fields.items():
         lines.append('printf("%s %%zu\\n", sizeof(%s));' % (cname, cname))
