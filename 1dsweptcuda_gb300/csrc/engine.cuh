@@ -109,8 +109,21 @@ __device__ __forceinline__ Ends tile_ends(int64_t base, int64_t nx, int W, int R
 
 // One Heat / KS sub-step of parity `par` (1: predictor / odd Heat step; 0:
 // corrector / even Heat step) at tile cell x.  (Euler levels run euler_level_tile / _warp.)
+//
+// FP64 Heat and KS form their general products on the integer pipe (mlq):
+// Heat both of its two, KS the sub-step's two (by dt, and the new value's
+// square).  A cell where one of them meets an operand or a product that path
+// does not take (a zero, a subnormal, an infinity, a NaN, a product near the
+// ends of the range) stores nothing and returns 1; the level's barrier
+// (level_barrier) then has the flagged cells computed on the FP64 pipe
+// (tile_point_pipe), from the same source rows, before any cell reads them.
+// The results are the same bits either way, and in the common case no FP64
+// instruction of that fallback is issued.
 template <int P, typename T>
-__device__ __forceinline__ void tile_point(const Params<T> &p, T *rows, int L, int par, int x, Ends e) {
+__host__ __device__ constexpr bool int_products() { return P != SW_EULER && sizeof(T) == 8; }
+
+template <int P, typename T>
+__device__ __forceinline__ uint32_t tile_point(const Params<T> &p, T *rows, int L, int par, int x, Ends e) {
     static_assert(P != SW_EULER, "Euler tile levels run euler_level_tile / euler_level_warp");
     constexpr int R = Scheme<P, T>::R;
     const T *src = rows + (par ^ 1) * L + R;
@@ -121,16 +134,64 @@ __device__ __forceinline__ void tile_point(const Params<T> &p, T *rows, int L, i
             if (x == e.first) l = x + 1;
             if (x == e.last) r = x - 1;
         }
-        dst[x] = heat_step(p, src[l], src[x], src[r]);
-    } else if constexpr (P == SW_KS) {
+        if constexpr (int_products<P, T>()) {
+            uint32_t bad = 0;
+            const T v = heat_step_q(p, src[l], src[x], src[r], bad);
+            if (!bad) dst[x] = v;
+            return bad;
+        } else {
+            dst[x] = heat_step(p, src[l], src[x], src[r]);
+            return 0;
+        }
+    } else {
         const T *sq = rows + (2 + (par ^ 1)) * L + R;  // squares of the source row
-        T v;
-        if (par)
-            v = ks_predict_sq(p, src[x - 2], src[x - 1], src[x], src[x + 1], src[x + 2], sq[x - 1], sq[x + 1]);
-        else
-            v = ks_correct_sq(p, dst[x], src[x - 2], src[x - 1], src[x], src[x + 1], src[x + 2], sq[x - 1], sq[x + 1]);
+        uint32_t bad = 0;
+        const T v = par ? ks_predict_q(p, src[x - 2], src[x - 1], src[x], src[x + 1], src[x + 2], sq[x - 1], sq[x + 1],
+                                       bad)
+                        : ks_correct_q(p, dst[x], src[x - 2], src[x - 1], src[x], src[x + 1], src[x + 2], sq[x - 1],
+                                       sq[x + 1], bad);
+        const T v2 = mlq(v, v, bad);
+        if (!bad) {
+            dst[x] = v;
+            rows[(2 + par) * L + R + x] = v2;
+        }
+        return bad;
+    }
+}
+// Cell x of a level on the FP64 pipe alone (the cells tile_point flagged).
+template <int P, typename T>
+__device__ __noinline__ void tile_point_pipe(const Params<T> &p, T *rows, int L, int par, int x, Ends e) {
+    constexpr int R = Scheme<P, T>::R;
+    if constexpr (P == SW_HEAT && int_products<P, T>()) {
+        const T *src = rows + (par ^ 1) * L + R;
+        int l = x - 1, r = x + 1;
+        if (p.bc != SW_BC_PERIODIC) {
+            if (x == e.first) l = x + 1;
+            if (x == e.last) r = x - 1;
+        }
+        rows[par * L + R + x] = heat_step(p, src[l], src[x], src[r]);
+    } else if constexpr (int_products<P, T>()) {
+        const T *src = rows + (par ^ 1) * L + R, *sq = rows + (2 + (par ^ 1)) * L + R;
+        T *dst = rows + par * L + R;
+        const T v = par ? ks_predict_sq(p, src[x - 2], src[x - 1], src[x], src[x + 1], src[x + 2], sq[x - 1], sq[x + 1])
+                        : ks_correct_sq(p, dst[x], src[x - 2], src[x - 1], src[x], src[x + 1], src[x + 2], sq[x - 1],
+                                        sq[x + 1]);
         dst[x] = v;
         rows[(2 + par) * L + R + x] = ml(v, v);
+    }
+}
+// The barrier that ends a level.  With integer-pipe products it also tells
+// whether any thread of the block flagged a cell; if one did, fix() computes
+// the flagged cells on the FP64 pipe and a second barrier follows.
+template <int P, typename T, typename Fix>
+__device__ __forceinline__ void level_barrier(uint32_t flagged, Fix &&fix) {
+    if constexpr (int_products<P, T>()) {
+        if (__syncthreads_or(flagged != 0)) {
+            fix();
+            __syncthreads();
+        }
+    } else {
+        __syncthreads();
     }
 }
 
@@ -491,35 +552,58 @@ enum TilePath { PATH_ANY = 0, PATH_CELL = 1, PATH_SPAN4 = 2 };
 // Heat / KS cells [lo, hi) of one level, one per thread from the lowest thread,
 // so the live cells start at thread 0: whole warps idle, not part-empty ones.
 // A block with a thread for every tile cell needs one pass (hi - lo <= W).
+// Returns the thread's flagged cells (tile_point), bit i for its i-th cell (a
+// thread has at most W / 32 <= 32 of them).
 template <int P, typename T>
-__device__ __forceinline__ void tile_cells(const Params<T> &p, T *rows, int L, int W, int par, int lo, int hi,
-                                           Ends e) {
+__device__ __forceinline__ uint32_t tile_cells(const Params<T> &p, T *rows, int L, int W, int par, int lo, int hi,
+                                               Ends e) {
+    uint32_t flagged = 0;
     if ((int)blockDim.x >= W) {
         const int x = lo + (int)threadIdx.x;
-        if (x < hi) tile_point<P, T>(p, rows, L, par, x, e);
+        if (x < hi) flagged = tile_point<P, T>(p, rows, L, par, x, e);
     } else {
-        for (int x = lo + (int)threadIdx.x; x < hi; x += blockDim.x) tile_point<P, T>(p, rows, L, par, x, e);
+        int i = 0;
+        for (int x = lo + (int)threadIdx.x; x < hi; x += blockDim.x, ++i)
+            flagged |= tile_point<P, T>(p, rows, L, par, x, e) << i;
+    }
+    return flagged;
+}
+template <int P, typename T>
+__device__ __forceinline__ void tile_cells_fix(const Params<T> &p, T *rows, int L, int par, int lo, int hi, Ends e,
+                                               uint32_t flagged) {
+    if constexpr (int_products<P, T>()) {
+        for (int x = lo + (int)threadIdx.x; x < hi && flagged; x += blockDim.x, flagged >>= 1)
+            if (flagged & 1u) tile_point_pipe<P, T>(p, rows, L, par, x, e);
     }
 }
 
 // One sub-step of parity `par` on tile cells [lo, hi).
+// Returns the thread's flagged cells (tile_cells).
 template <int P, typename T, int PATH>
-__device__ __forceinline__ void tile_level(const Params<T> &p, T *rows, int L, int W, int par, int lo, int hi,
-                                           Ends e) {
+__device__ __forceinline__ uint32_t tile_level(const Params<T> &p, T *rows, int L, int W, int par, int lo, int hi,
+                                               Ends e) {
     if constexpr (P == SW_EULER) {
         if constexpr (sizeof(T) == 8) euler_level_tile<T>(p, rows, L, par, lo, hi, e);
         else euler_level_warp<T>(p, rows, L, W, par, lo, hi, e);
     } else if constexpr (PATH == PATH_SPAN4) {
         tile_span4<P, T>(p, rows, L, par, lo, hi, e, (int)threadIdx.x);
     } else if constexpr (PATH == PATH_CELL) {
-        tile_cells<P, T>(p, rows, L, W, par, lo, hi, e);
+        return tile_cells<P, T>(p, rows, L, W, par, lo, hi, e);
     } else {
         if ((int)blockDim.x * 4 == W) {
             tile_span4<P, T>(p, rows, L, par, lo, hi, e, (int)threadIdx.x);
         } else {
-            tile_cells<P, T>(p, rows, L, W, par, lo, hi, e);
+            return tile_cells<P, T>(p, rows, L, W, par, lo, hi, e);
         }
     }
+    return 0;
+}
+// A Heat / KS level and the barrier after it.
+template <int P, typename T, int PATH>
+__device__ __forceinline__ void tile_level_sync(const Params<T> &p, T *rows, int L, int W, int par, int lo, int hi,
+                                                Ends e) {
+    const uint32_t flagged = tile_level<P, T, PATH>(p, rows, L, W, par, lo, hi, e);
+    level_barrier<P, T>(flagged, [&] { tile_cells_fix<P, T>(p, rows, L, par, lo, hi, e, flagged); });
 }
 
 // Heat and KS take the level loops two levels at a time, so each level's
@@ -540,10 +624,8 @@ __device__ __forceinline__ void tile_down(const Params<T> &p, T *rows, int L, in
         return;
     }
     for (int j = 1; j < H; j += 2) {
-        tile_level<P, T, PATH>(p, rows, L, W, 1, h - j * R, h + j * R, e);
-        __syncthreads();
-        tile_level<P, T, PATH>(p, rows, L, W, 0, h - (j + 1) * R, h + (j + 1) * R, e);
-        __syncthreads();
+        tile_level_sync<P, T, PATH>(p, rows, L, W, 1, h - j * R, h + j * R, e);
+        tile_level_sync<P, T, PATH>(p, rows, L, W, 0, h - (j + 1) * R, h + (j + 1) * R, e);
     }
 }
 // Up part: sub-steps u = 1..H-1 on the shrinking [uR, W - uR).
@@ -561,13 +643,10 @@ __device__ __forceinline__ void tile_up(const Params<T> &p, T *rows, int L, int 
     }
     int u = 1;
     for (; u + 1 < H; u += 2) {
-        tile_level<P, T, PATH>(p, rows, L, W, 1, u * R, W - u * R, e);
-        __syncthreads();
-        tile_level<P, T, PATH>(p, rows, L, W, 0, (u + 1) * R, W - (u + 1) * R, e);
-        __syncthreads();
+        tile_level_sync<P, T, PATH>(p, rows, L, W, 1, u * R, W - u * R, e);
+        tile_level_sync<P, T, PATH>(p, rows, L, W, 0, (u + 1) * R, W - (u + 1) * R, e);
     }
-    tile_level<P, T, PATH>(p, rows, L, W, 1, u * R, W - u * R, e);  // u = H - 1, odd
-    __syncthreads();
+    tile_level_sync<P, T, PATH>(p, rows, L, W, 1, u * R, W - u * R, e);  // u = H - 1, odd
 }
 
 // Default threads per swept block.  FP32 Heat / KS run 4 contiguous cells per
@@ -646,6 +725,22 @@ __global__ void __launch_bounds__(Scheme<P, T>::MAXT, (swept_min_blocks<P, T, PA
 // One classic sub-step at cell g of a domain of p.nx cells: classicHeat
 // (Heat1D_SweptShared.cu:132-145), classicKS (KS1D_SweptShared.cu:189-207),
 // classicEuler (Euler1D_SweptShared.cu:400-426).
+// A KS cell of the classic step on the FP64 pipe alone (a cell whose
+// integer-pipe products were flagged, as in tile_point).
+template <typename T>
+__device__ __noinline__ void classic_ks_pipe(const Params<T> &p, const T *__restrict__ in, T *__restrict__ out,
+                                             const int sub, const int64_t g) {
+    const int64_t nx = p.nx;
+    T v[5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) v[k] = in[wrap_pos(g - 2 + k, nx)];
+    out[g] = sub == 0 ? ks_predict(p, v[0], v[1], v[2], v[3], v[4]) : ks_correct(p, out[g], v[0], v[1], v[2], v[3], v[4]);
+}
+template <typename T>
+__device__ __noinline__ void classic_heat_pipe(const Params<T> &p, const T *__restrict__ in, T *__restrict__ out,
+                                               const int64_t l, const int64_t g, const int64_t r) {
+    out[g] = heat_step(p, in[l], in[g], in[r]);
+}
 template <int P, typename T>
 __device__ __forceinline__ void classic_cell(const Params<T> &p, const typename Scheme<P, T>::G *__restrict__ in,
                                              typename Scheme<P, T>::G *__restrict__ out, const int sub,
@@ -660,7 +755,14 @@ __device__ __forceinline__ void classic_cell(const Params<T> &p, const typename 
             if (g == 0) l = 1;
             if (g == nx - 1) r = nx - 2;
         }
-        out[g] = heat_step(p, in[l], in[g], in[r]);
+        if constexpr (int_products<P, T>()) {  // both products on the integer pipe (tile_point)
+            uint32_t bad = 0;
+            const T o = heat_step_q(p, in[l], in[g], in[r], bad);
+            if (__any_sync(__activemask(), bad != 0) && bad) classic_heat_pipe(p, in, out, l, g, r);
+            else out[g] = o;
+        } else {
+            out[g] = heat_step(p, in[l], in[g], in[r]);
+        }
     } else if constexpr (P == SW_KS) {
         T v[5];
         if (g >= 2 && g < nx - 2) {  // interior: no wrap
@@ -670,10 +772,18 @@ __device__ __forceinline__ void classic_cell(const Params<T> &p, const typename 
 #pragma unroll
             for (int k = 0; k < 5; ++k) v[k] = in[wrap_pos(g - 2 + k, nx)];
         }
-        if (sub == 0)
+        if constexpr (int_products<P, T>()) {  // the three products on the integer pipe (tile_point)
+            uint32_t bad = 0;
+            const T l2 = mlq(v[1], v[1], bad), r2 = mlq(v[3], v[3], bad);
+            const T o = sub == 0 ? ks_predict_q(p, v[0], v[1], v[2], v[3], v[4], l2, r2, bad)
+                                 : ks_correct_q(p, out[g], v[0], v[1], v[2], v[3], v[4], l2, r2, bad);
+            if (__any_sync(__activemask(), bad != 0) && bad) classic_ks_pipe(p, in, out, sub, g);
+            else out[g] = o;
+        } else if (sub == 0) {
             out[g] = ks_predict(p, v[0], v[1], v[2], v[3], v[4]);
-        else
+        } else {
             out[g] = ks_correct(p, out[g], v[0], v[1], v[2], v[3], v[4]);
+        }
     } else {
         if (g == 0 || g == nx - 1) {
             const int side = (g == 0) ? 0 : 1;
@@ -780,8 +890,8 @@ __device__ __forceinline__ int group_slot(int t, int n) {
     return k;
 }
 template <int P, typename T, int G, int PATH>
-__device__ __forceinline__ void group_level(const Params<T> &p, T *rows, int TS, int L, int par, int lo, int hi,
-                                            const Ends (&e)[G]) {
+__device__ __forceinline__ uint32_t group_level(const Params<T> &p, T *rows, int TS, int L, int par, int lo, int hi,
+                                                const Ends (&e)[G]) {
     // threads per tile at this level
     const int n = (PATH == PATH_SPAN4) ? ((hi - (lo & ~3) + 3) >> 2) : (hi - lo);
     const int t = (int)threadIdx.x;
@@ -792,8 +902,33 @@ __device__ __forceinline__ void group_level(const Params<T> &p, T *rows, int TS,
         for (int q = 1; q < G; ++q)
             if (k == q) ek = e[q];
         if constexpr (PATH == PATH_SPAN4) tile_span4<P, T>(p, rows + k * TS, L, par, lo, hi, ek, t - k * n);
-        else tile_point<P, T>(p, rows + k * TS, L, par, lo + t - k * n, ek);
+        else return tile_point<P, T>(p, rows + k * TS, L, par, lo + t - k * n, ek);
     }
+    return 0;
+}
+// A grouped level and the barrier after it (level_barrier); the extra() of the
+// last level (the fence before the bulk export) runs before that barrier.
+template <int P, typename T, int G, int PATH, typename Extra>
+__device__ __forceinline__ void group_level_sync(const Params<T> &p, T *rows, int TS, int L, int par, int lo, int hi,
+                                                 const Ends (&e)[G], Extra &&extra) {
+    const uint32_t flagged = group_level<P, T, G, PATH>(p, rows, TS, L, par, lo, hi, e);
+    extra();
+    level_barrier<P, T>(flagged, [&] {
+        if (flagged) {
+            const int n = hi - lo, t = (int)threadIdx.x, k = group_slot<G>(t, n);
+            Ends ek = e[0];
+#pragma unroll
+            for (int q = 1; q < G; ++q)
+                if (k == q) ek = e[q];
+            tile_point_pipe<P, T>(p, rows + k * TS, L, par, lo + t - k * n, ek);
+        }
+        extra();
+    });
+}
+template <int P, typename T, int G, int PATH>
+__device__ __forceinline__ void group_level_sync(const Params<T> &p, T *rows, int TS, int L, int par, int lo, int hi,
+                                                 const Ends (&e)[G]) {
+    group_level_sync<P, T, G, PATH>(p, rows, TS, L, par, lo, hi, e, [] {});
 }
 
 // FP64 KS tiles move their slots (and the up-triangle its state) by bulk
@@ -857,8 +992,7 @@ __device__ __forceinline__ void group_bulk_export(T *slots, T *rows, int TS, int
                                                   const int64_t (&hr)[G]) {
     constexpr int R = Scheme<P, T>::R;
     const int h = W >> 1;
-    fence_smem_for_bulk();  // this thread's row writes, visible to the copy engine
-    __syncthreads();
+    // the caller's last level fenced every thread's row writes and synchronised
     if (threadIdx.x == 0) {
         const unsigned piece = (unsigned)(h * sizeof(T));
 #pragma unroll
@@ -903,10 +1037,8 @@ __device__ __forceinline__ void swept_tile_group(const Params<T> &p, T *__restri
     __syncthreads();
     if constexpr (MODE != MODE_UP) {  // down part, two levels per iteration (H is even)
         for (int j = 1; j < H; j += 2) {
-            group_level<P, T, G, PATH>(p, rows, TS, L, 1, h - j * R, h + j * R, e);
-            __syncthreads();
-            group_level<P, T, G, PATH>(p, rows, TS, L, 0, h - (j + 1) * R, h + (j + 1) * R, e);
-            __syncthreads();
+            group_level_sync<P, T, G, PATH>(p, rows, TS, L, 1, h - j * R, h + j * R, e);
+            group_level_sync<P, T, G, PATH>(p, rows, TS, L, 0, h - (j + 1) * R, h + (j + 1) * R, e);
         }
     }
     if constexpr (MODE == MODE_DOWN) {
@@ -917,16 +1049,15 @@ __device__ __forceinline__ void swept_tile_group(const Params<T> &p, T *__restri
     } else {
         int u = 1;
         for (; u + 1 < H; u += 2) {
-            group_level<P, T, G, PATH>(p, rows, TS, L, 1, u * R, W - u * R, e);
-            __syncthreads();
-            group_level<P, T, G, PATH>(p, rows, TS, L, 0, (u + 1) * R, W - (u + 1) * R, e);
-            __syncthreads();
+            group_level_sync<P, T, G, PATH>(p, rows, TS, L, 1, u * R, W - u * R, e);
+            group_level_sync<P, T, G, PATH>(p, rows, TS, L, 0, (u + 1) * R, W - (u + 1) * R, e);
         }
-        group_level<P, T, G, PATH>(p, rows, TS, L, 1, u * R, W - u * R, e);  // u = H - 1
         if constexpr (group_bulk<P, T, PATH>()) {
+            // u = H - 1; each thread's row writes made visible to the copy engine before the barrier
+            group_level_sync<P, T, G, PATH>(p, rows, TS, L, 1, u * R, W - u * R, e, [] { fence_smem_for_bulk(); });
             group_bulk_export<P, T, G>(slots, rows, TS, L, W, hl, hr);
         } else {
-            __syncthreads();
+            group_level_sync<P, T, G, PATH>(p, rows, TS, L, 1, u * R, W - u * R, e);  // u = H - 1
             for (int i = threadIdx.x; i < G * W; i += blockDim.x) {
                 const int k = i / W, x = i - k * W;
                 tile_export_at<P, T>(rows + k * TS, L, W, slots + hl[k] * W, slots + hr[k] * W, x);

@@ -1,4 +1,4 @@
-// Two FP64 products formed on the integer pipe, rounded exactly as the FP64
+// FP64 products formed on the integer pipe, rounded exactly as the FP64
 // multiply rounds them (IEEE 754 binary64, round to nearest even).
 //
 // On GB300 an FP64 warp instruction holds its SM sub-partition's FP64 pipe for
@@ -91,6 +91,56 @@ SW_HD double mul6(double x) {
         return f64_from_bits((b & 0x8000000000000000ull) | ((uint64_t)ex << 52) | (q & 0x000fffffffffffffull));
     }
     return f64_mul_pipe(x, 6.0);
+}
+
+// ---- the general product on the integer pipe
+//
+// mul_int_fast(x, y, bad) = x * y, rounded once, for normal operands whose
+// product is normal (biased exponent at most 2045 before rounding).  The two
+// significands, each shifted to bit 63, give a 128-bit product whose upper
+// word holds the leading 64 bits (the leading one at bit 63 or 62); the lower
+// word only decides whether the discarded part is zero (the sticky bit of
+// round to nearest, ties to even).  For anything else -- zeros, subnormals,
+// infinities, NaNs, a product near or outside the ends of the normal range --
+// it sets bad and its result is meaningless: the caller recomputes that value
+// with the FP64 multiply.  No FP64 instruction sits on its path, so none is
+// issued: a predicated-off FP64 instruction still holds the FP64 pipe, and a
+// fallback inside this function measured as slow as the multiply it replaces.
+// The check is kept to three comparisons: the integer pipe is nearly as busy
+// as the FP64 pipe in the KS kernels, and handling zeros here (rare in those
+// products) cost more than it saved.
+// mul_int(x, y) is the same product with that fallback inside (host checks).
+SW_HD uint64_t umulhi64(uint64_t a, uint64_t b) {
+#if defined(__CUDA_ARCH__)
+    return __umul64hi(a, b);
+#else
+    return (uint64_t)(((unsigned __int128)a * b) >> 64);
+#endif
+}
+
+constexpr uint64_t kSign = 0x8000000000000000ull, kAbs = 0x7fffffffffffffffull;
+constexpr uint64_t kMant = 0x000fffffffffffffull, kHidden = 0x0010000000000000ull;
+
+SW_HD double mul_int_fast(double x, double y, uint32_t &bad) {
+    const uint64_t a = f64_bits(x), b = f64_bits(y);
+    const int ea = (int)(a >> 52) & 0x7ff, eb = (int)(b >> 52) & 0x7ff;
+    const uint64_t A = ((a & kMant) | kHidden) << 11, B = ((b & kMant) | kHidden) << 11;
+    const uint64_t hi = umulhi64(A, B), lo = A * B;
+    const int top = (int)(hi >> 63);  // the product's leading one at bit 127 (else 126)
+    const uint64_t n = top ? hi : (hi << 1) | (lo >> 63), below = top ? lo : lo << 1;
+    uint64_t m = n >> 11;
+    const uint32_t rem = (uint32_t)n & 0x7ffu;
+    m += (uint64_t)((rem > 0x400u) | ((rem == 0x400u) & ((below != 0) | ((uint32_t)m & 1u))));
+    const int er = ea + eb - 1023 + top;
+    // er <= 2045: a rounding carry leaves the exponent field at most 2046
+    bad |= (uint32_t)!((unsigned)(ea - 1) < 2046u && (unsigned)(eb - 1) < 2046u && (unsigned)(er - 1) < 2045u);
+    return f64_from_bits(((a ^ b) & kSign) | (((uint64_t)(int64_t)(er - 1) << 52) + m));
+}
+
+SW_HD double mul_int(double x, double y) {
+    uint32_t bad = 0;
+    const double r = mul_int_fast(x, y, bad);
+    return bad ? f64_mul_pipe(x, y) : r;
 }
 
 }  // namespace sw

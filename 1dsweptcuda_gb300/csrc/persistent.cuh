@@ -179,6 +179,16 @@ __device__ __forceinline__ bool wait_slots_warp(const unsigned *flags, int64_t h
 
 constexpr int kKsWarpNodesPerBlock = 8;
 
+// The warp barrier that ends a level of a one-warp node: level_barrier's warp
+// form (a flagged lane computes its cell again on the FP64 pipe first).
+template <typename T, typename Fix>
+__device__ __forceinline__ void warp_level_barrier(uint32_t flagged, Fix &&fix) {
+    if constexpr (int_products<SW_KS, T>()) {
+        if (__any_sync(0xffffffffu, flagged != 0) && flagged) fix();
+    }
+    __syncwarp();
+}
+
 template <typename T>
 __device__ __forceinline__ bool ks_smem_node_tile(const Params<T> &p, T *__restrict__ state, T *__restrict__ slots,
                                                   unsigned *flags, int *status, T *rows, const int64_t q,
@@ -208,8 +218,9 @@ __device__ __forceinline__ bool ks_smem_node_tile(const Params<T> &p, T *__restr
     const Ends e{INT32_MIN / 2, INT32_MIN / 2};  // KS is periodic: no end cells
     if (q > 0) {
         for (int jl = 1; jl <= H; ++jl) {
-            if (x >= h - jl * R && x < h + jl * R) tile_point<SW_KS, T>(p, rows, L, jl & 1, x, e);
-            __syncwarp();
+            uint32_t flagged = 0;
+            if (x >= h - jl * R && x < h + jl * R) flagged = tile_point<SW_KS, T>(p, rows, L, jl & 1, x, e);
+            warp_level_barrier<T>(flagged, [&] { tile_point_pipe<SW_KS, T>(p, rows, L, jl & 1, x, e); });
         }
     }
     if (q == last) {
@@ -217,8 +228,9 @@ __device__ __forceinline__ bool ks_smem_node_tile(const Params<T> &p, T *__restr
         return true;
     }
     for (int u = 1; u < H; ++u) {
-        if (x >= u * R && x < W - u * R) tile_point<SW_KS, T>(p, rows, L, u & 1, x, e);
-        __syncwarp();
+        uint32_t flagged = 0;
+        if (x >= u * R && x < W - u * R) flagged = tile_point<SW_KS, T>(p, rows, L, u & 1, x, e);
+        warp_level_barrier<T>(flagged, [&] { tile_point_pipe<SW_KS, T>(p, rows, L, u & 1, x, e); });
     }
     if (x < h) {  // as tile_export
         sl[x] = tile_get<SW_KS, T>(rows, L, 0, x);

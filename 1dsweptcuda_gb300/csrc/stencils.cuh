@@ -64,12 +64,22 @@ SW_HD double ml6(double c) { return mul6(c); }
 SW_HD float ml6(float c) { return ml(6.0f, c); }
 SW_HD double mlp2(double x, double f, int k) { return mul_pow2(x, f, k); }
 SW_HD float mlp2(float x, float f, int) { return ml(x, f); }
+// A general FP64 product on the integer pipe (mul_int_fast): bad is set where
+// the value must be recomputed with ml.  FP32 multiplies.
+SW_HD double mlq(double a, double b, uint32_t &bad) { return mul_int_fast(a, b, bad); }
+SW_HD float mlq(float a, float b, uint32_t &) { return ml(a, b); }
 
 // ---------------------------------------------------------------- Heat
 // execFunc, Heat1D_SweptShared.cu:121-130: fourier*(T[l] + T[r]) + fourierTwo*T[c]
 template <typename T>
 SW_HD T heat_step(const Params<T> &p, T l, T c, T r) {
     return ad(ml(p.fo, ad(l, r)), ml(p.fo2, c));
+}
+// The same with both products on the integer pipe (mlq): in FP64 two FP64-pipe
+// operations per cell-update instead of four.
+template <typename T>
+SW_HD T heat_step_q(const Params<T> &p, T l, T c, T r, uint32_t &bad) {
+    return ad(mlq(p.fo, ad(l, r), bad), mlq(p.fo2, c, bad));
 }
 
 // ------------------------------------------------------------------ KS
@@ -123,6 +133,17 @@ SW_HD T ks_predict_sq(const Params<T> &p, T ll, T l, T c, T r, T rr, T l2, T r2)
 template <typename T>
 SW_HD T ks_correct_sq(const Params<T> &p, T u, T ll, T l, T c, T r, T rr, T l2, T r2) {
     return ad(u, ml(-p.dt, ks_rhs_sq(p, ll, l, c, r, rr, l2, r2)));
+}
+// The same with the product by dt/2 or -dt on the integer pipe (mlq): in FP64
+// 10 FP64-pipe operations per sub-step instead of 11, the cell's square being
+// the other product a sub-step needs (engine.cuh forms it with mlq as well).
+template <typename T>
+SW_HD T ks_predict_q(const Params<T> &p, T ll, T l, T c, T r, T rr, T l2, T r2, uint32_t &bad) {
+    return sb(c, mlq(p.dth, ks_rhs_sq(p, ll, l, c, r, rr, l2, r2), bad));
+}
+template <typename T>
+SW_HD T ks_correct_q(const Params<T> &p, T u, T ll, T l, T c, T r, T rr, T l2, T r2, uint32_t &bad) {
+    return ad(u, mlq(-p.dt, ks_rhs_sq(p, ll, l, c, r, rr, l2, r2), bad));
 }
 
 // ------------------------------------------------- paired FP32 (sm_100+)

@@ -172,6 +172,60 @@ def test_ks_variant_32_cell_nodes(sw, solver, oracle):
     _assert_identical(got, want, "ks variant")
 
 
+def _nonnormal_ic(problem, nx, seed):
+    """A state whose products leave the integer pipe's range: subnormal cells
+    (1e-310), zeros, cells whose KS squares are subnormal (1e-160) or overflow
+    (1e155), and for Heat three neighbouring cells of 1.7e308 (the middle
+    one's neighbours' sum overflows), among ordinary values."""
+    rng = np.random.default_rng(seed)
+    x = np.arange(nx)
+    if problem == HEAT:
+        u = 50 + 40 * np.sin(2 * np.pi * x / nx) + rng.standard_normal(nx)
+        specials = ((1e-310, 24), (-3e-312, 8), (0.0, 16), (-0.0, 8), (1.7e308, 1))
+    else:
+        u = np.cos(2 * np.pi * 3 * x / nx) + 0.1 * rng.standard_normal(nx)
+        specials = ((1e-310, 24), (-3e-312, 8), (1e-160, 24), (0.0, 16), (-0.0, 8), (1e155, 1))
+    for value, count in specials:
+        u[rng.choice(nx, count, replace=False)] = value
+    if problem == HEAT:  # a cell whose neighbours' sum overflows
+        k = int(np.argmax(u))
+        u[(k + 1) % nx] = u[(k + 2) % nx] = u[k]
+    return u
+
+
+def _assert_same_or_both_nan(a, b, what):
+    """Bit-identical where finite or infinite; NaN where the other is NaN (the
+    payload and sign of a NaN differ between the CPU and the GPU)."""
+    na, nb = np.isnan(a), np.isnan(b)
+    assert np.array_equal(na, nb), "%s: NaN at different cells" % what
+    assert na.sum() < a.size // 4, "%s: too many NaN cells for a meaningful check" % what
+    _assert_identical(np.where(na, 0.0, a), np.where(nb, 0.0, b), what)
+
+
+@pytest.mark.parametrize("problem, alg, nx, tpb, bc", [
+    (KS, CLASSIC, 4096, 64, 0), (KS, SWEPT, 4096, 64, 0), (KS, SWEPT, 16384, 1024, 0), (KS, SWEPT, 65536, 64, 0),
+    (KS, SWEPT, 262144, 256, 0), (KS, VARIANT, 4096, 64, 0),
+    (HEAT, CLASSIC, 4096, 64, 0), (HEAT, CLASSIC, 4096, 64, 2), (HEAT, SWEPT, 4096, 64, 0), (HEAT, SWEPT, 4096, 64, 2),
+    (HEAT, SWEPT, 16384, 1024, 0), (HEAT, SWEPT, 32768, 32, 0), (HEAT, SWEPT, 65536, 64, 2), (HEAT, VARIANT, 4096, 64, 0),
+    (HEAT, VARIANT, 4096, 128, 2)])
+def test_fp64_values_outside_the_integer_products(sw, solver, oracle, problem, alg, nx, tpb, bc):
+    """FP64 Heat and KS form their general products on the integer pipe and
+    compute a cell again on the FP64 pipe where an operand or a product is
+    outside that path's range.  With such values in the state every path
+    (classic, one tile per block, two cells per thread at tpb 1024, grouped
+    tiles, the persistent variant and KS's 32-cell nodes; insulated and
+    periodic Heat) still gives the oracle's bits."""
+    dt = PROBLEM_DT[problem]
+    c = _case(oracle, problem, 8, nx, dt, bc=oracle.BC_PERIODIC if bc == 2 else None)
+    ic = _nonnormal_ic(problem, nx, seed=nx + tpb + bc)
+    q = tpb // (2 * oracle.RADIUS[problem] * oracle.SUBSTEPS[problem])
+    for nsteps in (q, 2 * q + 3):
+        want = oracle.classic(c, ic, nsteps)
+        got, _ = _gpu(sw, solver, problem, 8, alg, nx, tpb, dt, nsteps, ic, bc=bc)
+        _assert_same_or_both_nan(got, want, "problem %d alg %d nx %d tpb %d bc %d steps %d" % (
+            problem, alg, nx, tpb, bc, nsteps))
+
+
 @pytest.mark.parametrize("problem", [HEAT, KS, EULER])
 def test_reference_time_mode_snapshots(sw, solver, oracle, problem):
     """SW_TIME_REFERENCE: snapshots at the reference's output times hold the
