@@ -119,10 +119,24 @@ __device__ __forceinline__ Ends tile_ends(int64_t base, int64_t nx, int W, int R
 // (tile_point_pipe), from the same source rows, before any cell reads them.
 // The results are the same bits either way, and in the common case no FP64
 // instruction of that fallback is issued.
-template <int P, typename T>
-__host__ __device__ constexpr bool int_products() { return P != SW_EULER && sizeof(T) == 8; }
+//
+// Which cell mapping a kernel carries: PATH_ANY picks at run time (blockDim.x
+// * 4 == W: 4 cells per thread), PATH_CELL and PATH_SPAN4 hold only one, so a
+// kernel does not pay the registers of a path it never runs.  PATH_CELL_FP is
+// PATH_CELL with every product on the FP64 pipe: for domains of few tiles, where
+// each SM holds one or two tiles and a level's dependent chain is not hidden by
+// other tiles' work, the integer products' longer chain costs more than the
+// FP64 pipe time they free (Heat FP64 periodic, 32 tiles of 128 cells: 6.0e9
+// cell-updates/s with them, 8.4e9 without).  Euler always runs
+// euler_level_tile (FP64) or euler_level_warp (FP32).
+enum TilePath { PATH_ANY = 0, PATH_CELL = 1, PATH_SPAN4 = 2, PATH_CELL_FP = 3 };
 
-template <int P, typename T>
+template <int P, typename T, int PATH = PATH_ANY>
+__host__ __device__ constexpr bool int_products() {
+    return P != SW_EULER && sizeof(T) == 8 && PATH != PATH_CELL_FP;
+}
+
+template <int P, typename T, int PATH = PATH_ANY>
 __device__ __forceinline__ uint32_t tile_point(const Params<T> &p, T *rows, int L, int par, int x, Ends e) {
     static_assert(P != SW_EULER, "Euler tile levels run euler_level_tile / euler_level_warp");
     constexpr int R = Scheme<P, T>::R;
@@ -134,7 +148,7 @@ __device__ __forceinline__ uint32_t tile_point(const Params<T> &p, T *rows, int 
             if (x == e.first) l = x + 1;
             if (x == e.last) r = x - 1;
         }
-        if constexpr (int_products<P, T>()) {
+        if constexpr (int_products<P, T, PATH>()) {
             uint32_t bad = 0;
             const T v = heat_step_q(p, src[l], src[x], src[r], bad);
             if (!bad) dst[x] = v;
@@ -143,6 +157,14 @@ __device__ __forceinline__ uint32_t tile_point(const Params<T> &p, T *rows, int 
             dst[x] = heat_step(p, src[l], src[x], src[r]);
             return 0;
         }
+    } else if constexpr (!int_products<P, T, PATH>()) {
+        const T *sq = rows + (2 + (par ^ 1)) * L + R;  // squares of the source row
+        const T v = par ? ks_predict_sq(p, src[x - 2], src[x - 1], src[x], src[x + 1], src[x + 2], sq[x - 1], sq[x + 1])
+                        : ks_correct_sq(p, dst[x], src[x - 2], src[x - 1], src[x], src[x + 1], src[x + 2], sq[x - 1],
+                                        sq[x + 1]);
+        dst[x] = v;
+        rows[(2 + par) * L + R + x] = ml(v, v);
+        return 0;
     } else {
         const T *sq = rows + (2 + (par ^ 1)) * L + R;  // squares of the source row
         uint32_t bad = 0;
@@ -183,9 +205,9 @@ __device__ __noinline__ void tile_point_pipe(const Params<T> &p, T *rows, int L,
 // The barrier that ends a level.  With integer-pipe products it also tells
 // whether any thread of the block flagged a cell; if one did, fix() computes
 // the flagged cells on the FP64 pipe and a second barrier follows.
-template <int P, typename T, typename Fix>
+template <int P, typename T, int PATH, typename Fix>
 __device__ __forceinline__ void level_barrier(uint32_t flagged, Fix &&fix) {
-    if constexpr (int_products<P, T>()) {
+    if constexpr (int_products<P, T, PATH>()) {
         if (__syncthreads_or(flagged != 0)) {
             fix();
             __syncthreads();
@@ -543,35 +565,29 @@ __device__ __forceinline__ void euler_level_tile(const Params<T> &p, T *rows, in
     }
 }
 
-// Which cell mapping a kernel carries: PATH_ANY picks at run time (blockDim.x
-// * 4 == W: 4 cells per thread), PATH_CELL and PATH_SPAN4 hold only one, so a
-// kernel does not pay the registers of a path it never runs.  Euler always
-// runs euler_level_tile (FP64) or euler_level_warp (FP32).
-enum TilePath { PATH_ANY = 0, PATH_CELL = 1, PATH_SPAN4 = 2 };
-
 // Heat / KS cells [lo, hi) of one level, one per thread from the lowest thread,
 // so the live cells start at thread 0: whole warps idle, not part-empty ones.
 // A block with a thread for every tile cell needs one pass (hi - lo <= W).
 // Returns the thread's flagged cells (tile_point), bit i for its i-th cell (a
 // thread has at most W / 32 <= 32 of them).
-template <int P, typename T>
+template <int P, typename T, int PATH>
 __device__ __forceinline__ uint32_t tile_cells(const Params<T> &p, T *rows, int L, int W, int par, int lo, int hi,
                                                Ends e) {
     uint32_t flagged = 0;
     if ((int)blockDim.x >= W) {
         const int x = lo + (int)threadIdx.x;
-        if (x < hi) flagged = tile_point<P, T>(p, rows, L, par, x, e);
+        if (x < hi) flagged = tile_point<P, T, PATH>(p, rows, L, par, x, e);
     } else {
         int i = 0;
         for (int x = lo + (int)threadIdx.x; x < hi; x += blockDim.x, ++i)
-            flagged |= tile_point<P, T>(p, rows, L, par, x, e) << i;
+            flagged |= tile_point<P, T, PATH>(p, rows, L, par, x, e) << i;
     }
     return flagged;
 }
-template <int P, typename T>
+template <int P, typename T, int PATH>
 __device__ __forceinline__ void tile_cells_fix(const Params<T> &p, T *rows, int L, int par, int lo, int hi, Ends e,
                                                uint32_t flagged) {
-    if constexpr (int_products<P, T>()) {
+    if constexpr (int_products<P, T, PATH>()) {
         for (int x = lo + (int)threadIdx.x; x < hi && flagged; x += blockDim.x, flagged >>= 1)
             if (flagged & 1u) tile_point_pipe<P, T>(p, rows, L, par, x, e);
     }
@@ -587,13 +603,13 @@ __device__ __forceinline__ uint32_t tile_level(const Params<T> &p, T *rows, int 
         else euler_level_warp<T>(p, rows, L, W, par, lo, hi, e);
     } else if constexpr (PATH == PATH_SPAN4) {
         tile_span4<P, T>(p, rows, L, par, lo, hi, e, (int)threadIdx.x);
-    } else if constexpr (PATH == PATH_CELL) {
-        return tile_cells<P, T>(p, rows, L, W, par, lo, hi, e);
+    } else if constexpr (PATH == PATH_CELL || PATH == PATH_CELL_FP) {
+        return tile_cells<P, T, PATH>(p, rows, L, W, par, lo, hi, e);
     } else {
         if ((int)blockDim.x * 4 == W) {
             tile_span4<P, T>(p, rows, L, par, lo, hi, e, (int)threadIdx.x);
         } else {
-            return tile_cells<P, T>(p, rows, L, W, par, lo, hi, e);
+            return tile_cells<P, T, PATH>(p, rows, L, W, par, lo, hi, e);
         }
     }
     return 0;
@@ -603,7 +619,7 @@ template <int P, typename T, int PATH>
 __device__ __forceinline__ void tile_level_sync(const Params<T> &p, T *rows, int L, int W, int par, int lo, int hi,
                                                 Ends e) {
     const uint32_t flagged = tile_level<P, T, PATH>(p, rows, L, W, par, lo, hi, e);
-    level_barrier<P, T>(flagged, [&] { tile_cells_fix<P, T>(p, rows, L, par, lo, hi, e, flagged); });
+    level_barrier<P, T, PATH>(flagged, [&] { tile_cells_fix<P, T, PATH>(p, rows, L, par, lo, hi, e, flagged); });
 }
 
 // Heat and KS take the level loops two levels at a time, so each level's
@@ -902,7 +918,7 @@ __device__ __forceinline__ uint32_t group_level(const Params<T> &p, T *rows, int
         for (int q = 1; q < G; ++q)
             if (k == q) ek = e[q];
         if constexpr (PATH == PATH_SPAN4) tile_span4<P, T>(p, rows + k * TS, L, par, lo, hi, ek, t - k * n);
-        else return tile_point<P, T>(p, rows + k * TS, L, par, lo + t - k * n, ek);
+        else return tile_point<P, T, PATH>(p, rows + k * TS, L, par, lo + t - k * n, ek);
     }
     return 0;
 }
@@ -913,7 +929,7 @@ __device__ __forceinline__ void group_level_sync(const Params<T> &p, T *rows, in
                                                  const Ends (&e)[G], Extra &&extra) {
     const uint32_t flagged = group_level<P, T, G, PATH>(p, rows, TS, L, par, lo, hi, e);
     extra();
-    level_barrier<P, T>(flagged, [&] {
+    level_barrier<P, T, PATH>(flagged, [&] {
         if (flagged) {
             const int n = hi - lo, t = (int)threadIdx.x, k = group_slot<G>(t, n);
             Ends ek = e[0];
@@ -1068,8 +1084,11 @@ __device__ __forceinline__ void swept_tile_group(const Params<T> &p, T *__restri
 
 // Two 1024-thread blocks per SM (32 registers): the FP64 levels need the
 // warps of both to keep the FP64 pipe fed across each level's barrier.
+#ifndef SW_GROUP_MIN_BLOCKS
+#define SW_GROUP_MIN_BLOCKS 2
+#endif
 template <int P, typename T, int MODE, int G, int PATH>
-__global__ void __launch_bounds__(1024, 2) k_swept_group(const Params<T> p, T *__restrict__ state,
+__global__ void __launch_bounds__(1024, SW_GROUP_MIN_BLOCKS) k_swept_group(const Params<T> p, T *__restrict__ state,
                                                       T *__restrict__ slots, const int W, const int phase) {
     extern __shared__ __align__(16) unsigned char sw_smem[];
     swept_tile_group<P, T, MODE, G, PATH>(p, state, slots, reinterpret_cast<T *>(sw_smem), W, phase,
@@ -1078,6 +1097,9 @@ __global__ void __launch_bounds__(1024, 2) k_swept_group(const Params<T> p, T *_
 
 // Grouped tiles pay where blocks are plentiful: a domain of at least this many tiles.
 constexpr int64_t kGroupMinTiles = 1024;
+#ifndef SW_KS_GROUP_THREADS
+#define SW_KS_GROUP_THREADS 1024
+#endif
 
 // ------------------------------------------------------------- launchers
 // The dynamic shared-memory limit above the 48 KB default, set once per
@@ -1272,6 +1294,15 @@ cudaError_t launch_swept_ks_warp(const Params<T> &p, int mode, int phase, T *st,
     return cudaGetLastError();
 }
 
+// A domain of fewer tiles than two per SM of the current device: its levels'
+// dependent chains are not hidden by other tiles' work (PATH_CELL_FP).
+inline bool few_tiles(int64_t ntiles) {
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        return false;
+    return ntiles < 2 * (int64_t)sms;
+}
+
 template <int P, typename T>
 cudaError_t launch_swept(const void *vp, int mode, int phase, void *state, void *slots, int64_t nx, int W,
                          int threads_req, cudaStream_t s) {
@@ -1299,13 +1330,16 @@ cudaError_t launch_swept(const void *vp, int mode, int phase, void *state, void 
             }
             return launch_swept_path<P, T, PATH_SPAN4>(p, mode, phase, st, sl, nx, W, threads, s);
         }
-        constexpr int kMaxThreads = (P == SW_KS) ? 1024 : 512;
+        constexpr int kMaxThreads = (P == SW_KS) ? SW_KS_GROUP_THREADS : 512;
         if (group && threads == W) {
             if (P == SW_KS && 4 * W <= kMaxThreads && ntiles % 4 == 0)
                 return launch_swept_group<P, T, 4, PATH_CELL>(p, mode, phase, st, sl, nx, W, threads, s);
             if (2 * W <= kMaxThreads && ntiles % 2 == 0)
                 return launch_swept_group<P, T, 2, PATH_CELL>(p, mode, phase, st, sl, nx, W, threads, s);
         }
+    }
+    if constexpr (int_products<P, T>()) {
+        if (few_tiles(nx / W)) return launch_swept_path<P, T, PATH_CELL_FP>(p, mode, phase, st, sl, nx, W, threads, s);
     }
     return launch_swept_path<P, T, PATH_CELL>(p, mode, phase, st, sl, nx, W, threads, s);
 }

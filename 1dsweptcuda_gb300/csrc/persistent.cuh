@@ -391,6 +391,10 @@ cudaError_t launch_persistent(const void *vp, void *state, void *slots, unsigned
     }
     if (span4_launch<P, T>(W, threads))
         return launch_persistent_path<P, T, PATH_SPAN4>(p, st, sl, flags, status, nx, W, threads, n_diamonds, s);
+    if constexpr (int_products<P, T>()) {
+        if (few_tiles(nx / W))
+            return launch_persistent_path<P, T, PATH_CELL_FP>(p, st, sl, flags, status, nx, W, threads, n_diamonds, s);
+    }
     return launch_persistent_path<P, T, PATH_CELL>(p, st, sl, flags, status, nx, W, threads, n_diamonds, s);
 }
 

@@ -207,14 +207,18 @@ def _assert_same_or_both_nan(a, b, what):
     (KS, SWEPT, 262144, 256, 0), (KS, VARIANT, 4096, 64, 0),
     (HEAT, CLASSIC, 4096, 64, 0), (HEAT, CLASSIC, 4096, 64, 2), (HEAT, SWEPT, 4096, 64, 0), (HEAT, SWEPT, 4096, 64, 2),
     (HEAT, SWEPT, 16384, 1024, 0), (HEAT, SWEPT, 32768, 32, 0), (HEAT, SWEPT, 65536, 64, 2), (HEAT, VARIANT, 4096, 64, 0),
-    (HEAT, VARIANT, 4096, 128, 2)])
+    (HEAT, VARIANT, 4096, 128, 2),
+    # 512 tiles: enough for the integer products on the one-tile-per-block and persistent kernels
+    (KS, SWEPT, 1 << 19, 1024, 0), (KS, VARIANT, 32768, 64, 0), (HEAT, SWEPT, 1 << 19, 1024, 2),
+    (HEAT, VARIANT, 32768, 64, 0)])
 def test_fp64_values_outside_the_integer_products(sw, solver, oracle, problem, alg, nx, tpb, bc):
     """FP64 Heat and KS form their general products on the integer pipe and
     compute a cell again on the FP64 pipe where an operand or a product is
-    outside that path's range.  With such values in the state every path
+    outside that path's range; domains of fewer tiles than two per SM keep
+    every product on the FP64 pipe.  With such values in the state every path
     (classic, one tile per block, two cells per thread at tpb 1024, grouped
-    tiles, the persistent variant and KS's 32-cell nodes; insulated and
-    periodic Heat) still gives the oracle's bits."""
+    tiles, the persistent variant and KS's 32-cell nodes, on few and on many
+    tiles; insulated and periodic Heat) still gives the oracle's bits."""
     dt = PROBLEM_DT[problem]
     c = _case(oracle, problem, 8, nx, dt, bc=oracle.BC_PERIODIC if bc == 2 else None)
     ic = _nonnormal_ic(problem, nx, seed=nx + tpb + bc)
