@@ -90,10 +90,6 @@ inline Params<T> make_params(const sw_config &c, const sw_constants &k) {
         int e = 0;
         std::frexp((double)p.d2, &e);  // d2 = 0.5 * 2^e
         p.d2_e = e - 1;
-        std::frexp((double)p.c4, &e);
-        p.c4_e = e - 1;
-        std::frexp((double)p.d4, &e);
-        p.d4_e = e - 1;
     }
     return p;
 }

@@ -1084,11 +1084,8 @@ __device__ __forceinline__ void swept_tile_group(const Params<T> &p, T *__restri
 
 // Two 1024-thread blocks per SM (32 registers): the FP64 levels need the
 // warps of both to keep the FP64 pipe fed across each level's barrier.
-#ifndef SW_GROUP_MIN_BLOCKS
-#define SW_GROUP_MIN_BLOCKS 2
-#endif
 template <int P, typename T, int MODE, int G, int PATH>
-__global__ void __launch_bounds__(1024, SW_GROUP_MIN_BLOCKS) k_swept_group(const Params<T> p, T *__restrict__ state,
+__global__ void __launch_bounds__(1024, 2) k_swept_group(const Params<T> p, T *__restrict__ state,
                                                       T *__restrict__ slots, const int W, const int phase) {
     extern __shared__ __align__(16) unsigned char sw_smem[];
     swept_tile_group<P, T, MODE, G, PATH>(p, state, slots, reinterpret_cast<T *>(sw_smem), W, phase,
@@ -1097,9 +1094,6 @@ __global__ void __launch_bounds__(1024, SW_GROUP_MIN_BLOCKS) k_swept_group(const
 
 // Grouped tiles pay where blocks are plentiful: a domain of at least this many tiles.
 constexpr int64_t kGroupMinTiles = 1024;
-#ifndef SW_KS_GROUP_THREADS
-#define SW_KS_GROUP_THREADS 1024
-#endif
 
 // ------------------------------------------------------------- launchers
 // The dynamic shared-memory limit above the 48 KB default, set once per
@@ -1330,7 +1324,7 @@ cudaError_t launch_swept(const void *vp, int mode, int phase, void *state, void 
             }
             return launch_swept_path<P, T, PATH_SPAN4>(p, mode, phase, st, sl, nx, W, threads, s);
         }
-        constexpr int kMaxThreads = (P == SW_KS) ? SW_KS_GROUP_THREADS : 512;
+        constexpr int kMaxThreads = (P == SW_KS) ? 1024 : 512;
         if (group && threads == W) {
             if (P == SW_KS && 4 * W <= kMaxThreads && ntiles % 4 == 0)
                 return launch_swept_group<P, T, 4, PATH_CELL>(p, mode, phase, st, sl, nx, W, threads, s);

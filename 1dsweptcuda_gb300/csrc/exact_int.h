@@ -143,82 +143,4 @@ SW_HD double mul_int(double x, double y) {
     return bad ? f64_mul_pipe(x, y) : r;
 }
 
-// ---- the sum on the integer pipe
-//
-// add_int_fast(x, y, bad) = x + y, rounded once to nearest even, for normal
-// operands whose sum is normal or an exact zero, formed from the operands'
-// bits by the classic binary floating-point adder (as in J. Hauser's Berkeley
-// SoftFloat): the operand of larger magnitude keeps its place; both 53-bit
-// significands get 9 guard bits (leading one at bit 61, so a carry fits at
-// bit 62); the smaller one is shifted right by the exponent difference with
-// every bit shifted out OR-ed into its lowest bit ("jamming"); the two are
-// added, or subtracted when the signs differ; the result is normalised with
-// its leading one at bit 63 and rounded at bit 11 to nearest, ties to even.
-// Jamming keeps rounding exact: when bits were shifted out the exponents
-// differ by at least 2, so the difference loses at most one leading bit and
-// the jammed bit, kept below the rounding position, only decides "above or
-// below the halfway point", as the discarded bits would.  x == -y gives +0,
-// as the IEEE sum does in round-to-nearest, and a zero operand gives the
-// other operand (two zeros: -0 only if both are -0).  Anything else -- a
-// subnormal, infinite or NaN operand, a result outside the normal range --
-// sets bad, and the caller computes the value with the FP64 add.
-SW_HD int clz64(uint64_t v) {
-#if defined(__CUDA_ARCH__)
-    return __clzll((long long)v);
-#else
-    return v ? __builtin_clzll(v) : 64;
-#endif
-}
-
-SW_HD double add_int_fast(double x, double y, uint32_t &bad) {
-    const uint64_t a = f64_bits(x), b = f64_bits(y);
-    const uint64_t ma = a & kAbs, mb = b & kAbs;
-    const bool swap = ma < mb;
-    const uint64_t mh = swap ? mb : ma, ml = swap ? ma : mb;  // magnitudes, |h| >= |l|
-    const int eh = (int)(mh >> 52), el = (int)(ml >> 52);
-    const uint64_t H = ((mh & kMant) | kHidden) << 9, Lg = ((ml & kMant) | kHidden) << 9;
-    const int d = eh - el < 63 ? eh - el : 63;  // from 63 on every bit of Lg is shifted out
-    const uint64_t Ls = (Lg >> d) | (uint64_t)(d != 0 && (Lg << ((64 - d) & 63)) != 0);
-    const uint64_t S = ((a ^ b) & kSign) ? H - Ls : H + Ls;
-    const int lz = clz64(S);
-    const uint64_t N = S << (lz & 63);  // leading one at bit 63
-    const int e = eh + 2 - lz;          // biased exponent of N's leading bit
-    uint64_t m = N >> 11;
-    const uint32_t rem = (uint32_t)N & 0x7ffu;
-    m += (uint64_t)((rem > 0x400u) | ((rem == 0x400u) & (uint32_t)m & 1u));
-    // e <= 2045: a rounding carry leaves the exponent field at most 2046
-    const bool zl = ml == 0;  // the smaller operand is a zero
-    bad |= (uint32_t)!(((unsigned)(eh - 1) < 2046u || mh == 0) && ((unsigned)(el - 1) < 2046u || zl) &&
-                       ((unsigned)(e - 1) < 2045u || S == 0 || zl));
-    const uint64_t r = ((swap ? b : a) & kSign) | (((uint64_t)(int64_t)(e - 1) << 52) + m);
-    return f64_from_bits(zl ? (mh == 0 ? (a & b) : (swap ? b : a)) : (S == 0 ? 0 : r));
-}
-
-// x * 2^k, exact, for a zero or for a normal x whose product is normal (|k|
-// small); sets bad otherwise.
-SW_HD double scale_fast(double x, int k, uint32_t &bad) {
-    const uint64_t b = f64_bits(x);
-    const int e = (int)((b >> 52) & 0x7ff);
-    const bool z = (b & kAbs) == 0;
-    bad |= (uint32_t)!(((unsigned)(e - 1) < 2046u && (unsigned)(e + k - 1) < 2046u) || z);
-    return f64_from_bits(z ? b : b + ((uint64_t)(int64_t)k << 52));
-}
-
-SW_HD double f64_add_pipe(double a, double b) {
-#if defined(__CUDA_ARCH__)
-    double r;
-    asm volatile("add.rn.f64 %0, %1, %2;" : "=d"(r) : "d"(a), "d"(b));
-    return r;
-#else
-    volatile double va = a;
-    return va + b;
-#endif
-}
-
-SW_HD double add_int(double x, double y) {
-    uint32_t bad = 0;
-    const double r = add_int_fast(x, y, bad);
-    return bad ? f64_add_pipe(x, y) : r;
-}
-
 }  // namespace sw

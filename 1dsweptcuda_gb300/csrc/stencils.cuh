@@ -68,25 +68,6 @@ SW_HD float mlp2(float x, float f, int) { return ml(x, f); }
 // the value must be recomputed with ml.  FP32 multiplies.
 SW_HD double mlq(double a, double b, uint32_t &bad) { return mul_int_fast(a, b, bad); }
 SW_HD float mlq(float a, float b, uint32_t &) { return ml(a, b); }
-// A general FP64 sum on the integer pipe (add_int_fast), bad set as by mlq.  FP32 adds.
-SW_HD double adq(double a, double b, uint32_t &bad) { return add_int_fast(a, b, bad); }
-SW_HD float adq(float a, float b, uint32_t &) { return ad(a, b); }
-// -x and x * 2^k (exact) from the bits
-SW_HD double ngb(double x) { return f64_from_bits(f64_bits(x) ^ kSign); }
-SW_HD float ngb(float x) { return -x; }
-
-// Which FP64 sums of a sub-step the integer pipe forms (bit i: the i-th sum
-// of heat_step_q / ks_rhs_q and the sub-step's final sum).  The integer pipe
-// then carries the sums with the products; the FP64 pipe keeps the rest, so
-// that the two pipes share the work.
-#ifndef SW_KS_INT_ADDS
-#define SW_KS_INT_ADDS 0x000u
-#endif
-#ifndef SW_HEAT_INT_ADDS
-#define SW_HEAT_INT_ADDS 0x0u
-#endif
-constexpr unsigned kKsIntAdds = SW_KS_INT_ADDS;
-constexpr unsigned kHeatIntAdds = SW_HEAT_INT_ADDS;
 
 // ---------------------------------------------------------------- Heat
 // execFunc, Heat1D_SweptShared.cu:121-130: fourier*(T[l] + T[r]) + fourierTwo*T[c]
@@ -98,9 +79,7 @@ SW_HD T heat_step(const Params<T> &p, T l, T c, T r) {
 // operations per cell-update instead of four.
 template <typename T>
 SW_HD T heat_step_q(const Params<T> &p, T l, T c, T r, uint32_t &bad) {
-    const T s = (kHeatIntAdds & 1u) ? adq(l, r, bad) : ad(l, r);
-    const T a = mlq(p.fo, s, bad), b = mlq(p.fo2, c, bad);
-    return (kHeatIntAdds & 2u) ? adq(a, b, bad) : ad(a, b);
+    return ad(mlq(p.fo, ad(l, r), bad), mlq(p.fo2, c, bad));
 }
 
 // ------------------------------------------------------------------ KS
@@ -155,48 +134,15 @@ template <typename T>
 SW_HD T ks_correct_sq(const Params<T> &p, T u, T ll, T l, T c, T r, T rr, T l2, T r2) {
     return ad(u, ml(-p.dt, ks_rhs_sq(p, ll, l, c, r, rr, l2, r2)));
 }
-// ks_rhs_sq under KS_POW2 (c4, d2, d4 powers of two) in FP64, with the sums
-// the mask kKsIntAdds names on the integer pipe (adq): each fused multiply-add
-// by a power of two is the sum of an exact product, which scale_fast forms
-// from the bits.  The same bits as ks_rhs_sq; bad set where a value must be
-// recomputed on the FP64 pipe.
-SW_HD double ks_rhs_q(const Params<double> &p, double ll, double l, double c, double r, double rr, double l2,
-                      double r2, uint32_t &bad) {
-    constexpr unsigned M = kKsIntAdds;
-    const double conv = (M & 1u) ? adq(r2, ngb(l2), bad) : sb(r2, l2);
-    const double s = (M & 2u) ? adq(l, r, bad) : ad(l, r);
-    const double sec = (M & 4u) ? adq(ngb(scale_fast(c, 1, bad)), s, bad) : fm(-2.0, c, s);
-    const double f1 = (M & 8u) ? adq(ngb(scale_fast(l, 2, bad)), ll, bad) : fm(-4.0, l, ll);
-    const double f2 = (M & 16u) ? adq(f1, ml6(c), bad) : ad(f1, ml6(c));
-    const double f3 = (M & 32u) ? adq(ngb(scale_fast(r, 2, bad)), f2, bad) : fm(-4.0, r, f2);
-    const double fourth = (M & 64u) ? adq(f3, rr, bad) : ad(f3, rr);
-    const double t1 = (M & 128u) ? adq(scale_fast(conv, p.c4_e, bad), scale_fast(sec, p.d2_e, bad), bad)
-                                 : fm(conv, p.c4, mlp2(sec, p.d2, p.d2_e));
-    return (M & 256u) ? adq(scale_fast(fourth, p.d4_e, bad), t1, bad) : fm(fourth, p.d4, t1);
-}
-// The sub-step with the product by dt/2 or -dt on the integer pipe (mlq): in
-// FP64 10 FP64-pipe operations per sub-step, the cell's square being the
-// other product a sub-step needs (engine.cuh forms it with mlq as well).
-// Under KS_POW2 the sums kKsIntAdds names move to the integer pipe too (bit 9:
-// the sub-step's final sum).
+// The same with the product by dt/2 or -dt on the integer pipe (mlq): in FP64
+// 10 FP64-pipe operations per sub-step instead of 11, the cell's square being
+// the other product a sub-step needs (engine.cuh forms it with mlq as well).
 template <typename T>
 SW_HD T ks_predict_q(const Params<T> &p, T ll, T l, T c, T r, T rr, T l2, T r2, uint32_t &bad) {
-    if constexpr (sizeof(T) == 8 && kKsIntAdds != 0u) {
-        if (p.ks_form == KS_POW2) {
-            const T d = mlq(p.dth, ks_rhs_q(p, ll, l, c, r, rr, l2, r2, bad), bad);
-            return (kKsIntAdds & 512u) ? adq(c, ngb(d), bad) : sb(c, d);
-        }
-    }
     return sb(c, mlq(p.dth, ks_rhs_sq(p, ll, l, c, r, rr, l2, r2), bad));
 }
 template <typename T>
 SW_HD T ks_correct_q(const Params<T> &p, T u, T ll, T l, T c, T r, T rr, T l2, T r2, uint32_t &bad) {
-    if constexpr (sizeof(T) == 8 && kKsIntAdds != 0u) {
-        if (p.ks_form == KS_POW2) {
-            const T d = mlq(-p.dt, ks_rhs_q(p, ll, l, c, r, rr, l2, r2, bad), bad);
-            return (kKsIntAdds & 512u) ? adq(u, d, bad) : ad(u, d);
-        }
-    }
     return ad(u, mlq(-p.dt, ks_rhs_sq(p, ll, l, c, r, rr, l2, r2), bad));
 }
 

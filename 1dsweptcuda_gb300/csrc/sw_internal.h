@@ -21,7 +21,7 @@ struct Params {
     int64_t nx;
     int bc;                    // SW_BC_MIRROR / PERIODIC / DIRICHLET
     int ks_form;               // KS: how c4, d2, d4 enter the right-hand side (enum KsForm)
-    int d2_e, c4_e, d4_e;      // KS_POW2: d2 = 2^d2_e, c4 = 2^c4_e, d4 = 2^d4_e
+    int d2_e;                  // KS_POW2: d2 = 2^d2_e
     T nz;                      // -0.0, the addend that makes an fma a plain product (paired FP32 path)
     int *status;               // device word a kernel sets when a bounded wait runs out (may be null)
 };

@@ -70,8 +70,9 @@ WORKLOAD = ("KS1D FP64 swept (alg 1), periodic, nx=2^20, tpb=256, dx=0.5, dt=0.0
             "(40000 time steps per step)")
 K40_KS_F64_SWEPT_PUBLISHED = 1.07e10  # the reference's published KS FP64 swept figure, nx=2^20, on a K40c
 # DRAM bytes (read + write) of one diamond launch of this workload, from the ncu capture
-# summarised in profiles/ks_f64_swept_diamond_nx2e20.md (cold-cache replay).
-DIAMOND_TRAFFIC_BYTES = 17640000
+# summarised in profiles/ks_f64_swept_diamond_nx2e20.md (cold-cache replay: 16.83 MB read,
+# 0.06 MB written).
+DIAMOND_TRAFFIC_BYTES = 16882176
 DIAMOND_TRAFFIC_SOURCE = "profiles/ks_f64_swept_diamond_nx2e20.md (ncu dram__bytes_read.sum + dram__bytes_write.sum)"
 
 
@@ -480,13 +481,17 @@ def run_ours(args) -> None:
     roof = {"bound": "fp64_pipe", "kernel": "k_swept_group<KS,double,DIAMOND,4> (four 256-cell tiles per block)",
             "achieved": ops / 1e12, "peak": mix_peak / 1e12, "unit": "Tops/s", "frac": ops / mix_peak,
             "peak_source": "measured live in this run (sw_fp64_rates) for the kernel's FP64 operation mix",
+            "note": "achieved counts the scheme's 24 FP64 operations per cell-update; 4 of them (the "
+                    "general products) run on the integer pipe with the same bits, so fp64_pipe.frac is the "
+                    "FP64 pipe's own utilisation",
             "ops_per_cell_update": KS_OPS_PER_UPDATE, "ops_mix_per_substep": KS_SUBSTEP_MIX,
             "fp64_rates_per_s": rates, "frac_of_dfma_rate": ops / rates["fma"],
             "fp64_pipe": {"ops_per_cell_update": KS_FP64_PIPE_OPS_PER_UPDATE, "achieved": pipe_ops / 1e12,
                           "peak": pipe_peak / 1e12, "frac": pipe_ops / pipe_peak,
                           "integer_pipe_products_per_cell_update": KS_OPS_PER_UPDATE - KS_FP64_PIPE_OPS_PER_UPDATE,
                           "note": "the operations the FP64 pipe itself issues: the two general products of a "
-                                  "sub-step run on the integer pipe with the same bits (mul_int_fast)"},
+                                  "sub-step (counted in the 24) run on the integer pipe with the same bits "
+                                  "(mul_int_fast), as do its two exact ones (mul6, mul_pow2; not counted)"},
             "launch_ms": launch_ms, "cell_updates_per_launch": updates,
             "traffic": DIAMOND_TRAFFIC_BYTES, "traffic_source": DIAMOND_TRAFFIC_SOURCE,
             "hbm": {"effective_gbs": alg_bytes / (launch_ms * 1e-3) / 1e9, "peak_gbs": hbm,
