@@ -93,7 +93,10 @@ int ensure_tables(sw_ctx *ctx, int32_t n, const int64_t *nx, int W) {
     if (!dom.empty()) SW_CUDA(ctx, cudaMemcpy(d_dom, dom.data(), sizeof(int32_t) * dom.size(), cudaMemcpyHostToDevice));
     int32_t *d_blk = d_dom + dom.size();
     if (!blk.empty()) SW_CUDA(ctx, cudaMemcpy(d_blk, blk.data(), sizeof(int32_t) * blk.size(), cudaMemcpyHostToDevice));
-    bt.dev = BatchDev{d_dom, d_off, d_tile0, d_blk, tiles, cells, n};
+    int32_t group = 4;  // grouped swept blocks (G tiles of one domain each) where every domain allows them
+    for (int32_t d = 0; d < n && W; ++d)
+        while (group > 1 && (nx[d] / W) % group != 0) group >>= 1;
+    bt.dev = BatchDev{d_dom, d_off, d_tile0, d_blk, tiles, cells, n, W ? group : 1};
     bt.nx.assign(nx, nx + n);
     bt.W = W;
     if (ctx->graph.exec) {  // the tables moved: a cached graph may point at the old ones
@@ -184,6 +187,7 @@ int run_batch_device(sw_ctx *ctx, const sw_config &c0, int32_t n, const int64_t 
     cd.nx = nx[0];
     sw_constants_of(&cd, &k);
     Params<T> p = sw::make_params<T>(cd, k);
+    p.status = ctx->d_status;  // bounded waits (grouped blocks' bulk copies) report here
 
     cudaStream_t s = ctx->stream;
     SW_CUDA(ctx, cudaEventRecord(ctx->e0, user));
@@ -240,6 +244,7 @@ int run_batch_device(sw_ctx *ctx, const sw_config &c0, int32_t n, const int64_t 
     SW_CUDA(ctx, cudaGetLastError());
     int st = 0;
     SW_CUDA(ctx, cudaMemcpy(&st, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost));
+    if (st == 2) return fail(ctx, SW_ERR_TIMEOUT, "ensemble swept kernel: a bulk copy's wait ran out");
     if (st) return fail(ctx, SW_ERR_TIMEOUT, "persistent ensemble kernel: an inter-block wait expired");
     float ms = 0;
     cudaEventElapsedTime(&ms, ctx->k0, ctx->k1);

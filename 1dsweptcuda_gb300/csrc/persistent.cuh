@@ -306,6 +306,23 @@ __global__ void __launch_bounds__(Scheme<P, T>::MAXT, (swept_min_blocks<P, T, PA
                            g - b.tile0[d]);
 }
 
+// G consecutive tiles of one domain per block (one cell per thread), as
+// k_swept_group runs a single domain: the batch's tile counts are all
+// multiples of G (BatchDev::group), so a block's tiles never straddle domains.
+template <int P, typename T, int MODE, int G, int PATH>
+__global__ void __launch_bounds__(1024, 2)
+    k_swept_batch_group(const Params<T> p, T *__restrict__ state, T *__restrict__ slots, const BatchDev b, const int W,
+                        const int phase) {
+    extern __shared__ __align__(16) unsigned char sw_smem[];
+    const int64_t g0 = G * (int64_t)blockIdx.x;
+    const int d = b.tile_dom[g0];
+    const int64_t off = b.off[d];
+    Params<T> q = p;
+    q.nx = b.off[d + 1] - off;
+    swept_tile_group<P, T, MODE, G, PATH>(q, state + off, slots + 2 * off, reinterpret_cast<T *>(sw_smem), W, phase,
+                                          g0 - b.tile0[d]);
+}
+
 // Classic step of an ensemble, one cell per thread, kClassicBlock threads per
 // block.  The table gives the domain of the block's first cell; each thread
 // walks forward from it, which is one compare when domains are longer than a
@@ -418,6 +435,29 @@ cudaError_t launch_swept_batch_path(const Params<T> &p, int mode, int phase, typ
     return cudaGetLastError();
 }
 
+template <int P, typename T, int G>
+cudaError_t launch_swept_batch_group(const Params<T> &p, int mode, int phase, T *st, T *sl, const BatchDev &b, int W,
+                                     cudaStream_t s) {
+    static SmemOnce once;
+    cudaError_t e = once.ensure(k_swept_batch_group<P, T, MODE_UP, G, PATH_CELL>,
+                                k_swept_batch_group<P, T, MODE_DIAMOND, G, PATH_CELL>,
+                                k_swept_batch_group<P, T, MODE_DOWN, G, PATH_CELL>);
+    if (e != cudaSuccess) return e;
+    const size_t smem = G * swept_smem_bytes<P, T>(W);
+    const unsigned grid = (unsigned)(b.n_tiles / G);
+    const int block = G * W;
+    switch (mode) {
+    case MODE_UP:
+        k_swept_batch_group<P, T, MODE_UP, G, PATH_CELL><<<grid, block, smem, s>>>(p, st, sl, b, W, phase);
+        break;
+    case MODE_DIAMOND:
+        k_swept_batch_group<P, T, MODE_DIAMOND, G, PATH_CELL><<<grid, block, smem, s>>>(p, st, sl, b, W, phase);
+        break;
+    default: k_swept_batch_group<P, T, MODE_DOWN, G, PATH_CELL><<<grid, block, smem, s>>>(p, st, sl, b, W, phase); break;
+    }
+    return cudaGetLastError();
+}
+
 template <int P, typename T>
 cudaError_t launch_swept_batch(const void *vp, int mode, int phase, void *state, void *slots, const void *bt, int W,
                                int threads, cudaStream_t s) {
@@ -426,6 +466,17 @@ cudaError_t launch_swept_batch(const void *vp, int mode, int phase, void *state,
     const BatchDev &b = *static_cast<const BatchDev *>(bt);
     threads = swept_threads_for<P, T>(W, threads);
     G *st = static_cast<G *>(state), *sl = static_cast<G *>(slots);
+    if constexpr (P != SW_EULER) {
+        // one cell per thread: G tiles of a domain per block, as the single-domain
+        // launcher groups them (KS four up to 1024 threads, Heat two up to 512)
+        constexpr int kMaxThreads = (P == SW_KS) ? 1024 : 512;
+        if (threads == W && !span4_launch<P, T>(W, threads)) {
+            if (P == SW_KS && 4 * W <= kMaxThreads && b.group % 4 == 0)
+                return launch_swept_batch_group<P, T, 4>(p, mode, phase, st, sl, b, W, s);
+            if (2 * W <= kMaxThreads && b.group % 2 == 0)
+                return launch_swept_batch_group<P, T, 2>(p, mode, phase, st, sl, b, W, s);
+        }
+    }
     if (span4_launch<P, T>(W, threads))
         return launch_swept_batch_path<P, T, PATH_SPAN4>(p, mode, phase, st, sl, b, W, threads, s);
     return launch_swept_batch_path<P, T, PATH_CELL>(p, mode, phase, st, sl, b, W, threads, s);

@@ -42,6 +42,7 @@ struct BatchDev {
     int64_t n_tiles;
     int64_t n_cells;
     int32_t n_dom;
+    int32_t group;  // the largest of 1, 2, 4 that divides every domain's tile count
 };
 constexpr int kClassicBlock = 256;  // threads (= cells) per block of the ensemble classic kernel
 

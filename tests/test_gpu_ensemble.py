@@ -34,6 +34,29 @@ def test_ks_ensemble_bit_exact(sw, solver, oracle, prec, alg):
     np.testing.assert_array_equal(out, want)
 
 
+@pytest.mark.parametrize("prec", [8, 4])
+def test_ensembles_of_grouped_tiles(sw, solver, oracle, prec):
+    """Every domain a multiple of four tiles (KS) or two (Heat), one cell per
+    thread: the swept passes run G tiles of one domain per block, as the
+    single-domain kernel groups them (FP64 KS with bulk-copied slots).  Every
+    domain still equals the oracle run on it alone."""
+    dt = np.float64 if prec == 8 else np.float32
+    nx, ic = ens.make_ensemble(n_domains=24, lo=8, hi=11, seed=7, dtype=dt)
+    cfg = sw.make_config(1, prec, alg=1, tpb=64, dt=0.005, time_mode=sw.TIME_STEPS, n_steps=52)
+    out, res = solver.run_batch(cfg, nx, ic)
+    assert res.n_steps == 52
+    np.testing.assert_array_equal(out, _oracle_each(oracle, 1, prec, nx, ic, 0.005, 52))
+    rng = np.random.default_rng(3)
+    nx = np.array([256, 128, 512, 128, 1024], dtype=np.int64)
+    ic = (rng.standard_normal(int(nx.sum())) + 10.0).astype(dt)
+    cfg = sw.make_config(0, prec, alg=1, tpb=64, dt=0.004, bc=sw.BC_PERIODIC, time_mode=sw.TIME_STEPS, n_steps=100)
+    out, _ = solver.run_batch(cfg, nx, ic)
+    np.testing.assert_array_equal(out, _oracle_each(oracle, 0, prec, nx, ic, 0.004, 100, bc=oracle.BC_PERIODIC))
+    cfg = sw.make_config(0, prec, alg=1, tpb=64, dt=0.004, time_mode=sw.TIME_STEPS, n_steps=100)  # insulated ends
+    out, _ = solver.run_batch(cfg, nx, ic)
+    np.testing.assert_array_equal(out, _oracle_each(oracle, 0, prec, nx, ic, 0.004, 100))
+
+
 def test_heat_periodic_and_euler_ensembles(sw, solver, oracle):
     rng = np.random.default_rng(1)
     nx = np.array([128, 512, 256, 1024, 128], dtype=np.int64)

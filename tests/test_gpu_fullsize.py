@@ -87,3 +87,21 @@ def test_sod_accuracy_gpu(sw, solver):
     ex = exact.sod(exact.sod_cell_centres(nx), steps * dt)
     err = float(np.mean(np.abs(q[1:-1, 0] - ex["density"])))
     assert err < 0.001, err
+
+
+@pytest.mark.parametrize("prec", [8, 4])
+def test_euler_2_22_swept_equals_oracle(sw, solver, oracle, prec):
+    """Euler Sod at config 3's size (nx=2^22, tpb=512, dt/dx=0.1): the swept run
+    over 256 steps (one up-triangle, diamonds, a down-triangle and classic
+    remainder steps) equals the oracle's classic scheme bit for bit, the oracle
+    on every host thread."""
+    nx, tpb, steps = 1 << 22, 512, 256 + 37
+    dt = 0.1 / (nx - 2)
+    cfg = sw.make_config(2, prec, alg=sw.ALG_SWEPT, nx=nx, tpb=tpb, dt=dt, time_mode=sw.TIME_STEPS, n_steps=steps)
+    ic = oracle.reference_ic(oracle.EULER, prec, nx)
+    want = oracle.classic(oracle.reference_consts(oracle.EULER, prec, nx, dt), ic, steps,
+                          threads=oracle.openmp_threads())
+    got, res, _ = solver.run(cfg, ic)
+    assert res.n_steps == steps
+    assert np.isfinite(got).all()
+    np.testing.assert_array_equal(got, want)
