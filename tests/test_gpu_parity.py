@@ -230,6 +230,37 @@ def test_fp64_values_outside_the_integer_products(sw, solver, oracle, problem, a
             problem, alg, nx, tpb, bc, nsteps))
 
 
+def _euler_special_ic(oracle, nx, seed):
+    """A Sod tube with edge-case states in places: momenta of +-1e-160 (their
+    squares underflow to subnormals), +-1e-310 (subnormal), zeros of both
+    signs, and density and energy jumps of one rounding unit."""
+    rng = np.random.default_rng(seed)
+    u = oracle.reference_ic(EULER, 8, nx).reshape(-1, 3).copy()
+    inner = np.arange(2, nx - 2)
+    for value, count in ((1e-160, 12), (-1e-160, 12), (1e-310, 6), (-3e-312, 6), (-0.0, 24)):
+        u[rng.choice(inner, count, replace=False), 1] = value
+    k = rng.choice(inner, 12, replace=False)
+    u[k, 0] *= 1 + 1e-15
+    u[k, 2] *= 1 - 1e-15
+    return u.ravel()
+
+
+@pytest.mark.parametrize("alg, nx, tpb", [(CLASSIC, 4096, 256), (SWEPT, 4096, 256), (VARIANT, 4096, 256),
+                                          (SWEPT, 1 << 16, 512), (VARIANT, 1 << 15, 256), (CLASSIC, 1 << 16, 512)])
+def test_euler_edge_case_states(sw, solver, oracle, alg, nx, tpb):
+    """Subnormal and underflowing momenta, signed zeros and one-ulp jumps in
+    a Sod tube: every FP64 Euler path (classic, swept on few and many tiles,
+    the persistent variant) gives the oracle's bits."""
+    dt = 0.1 / (nx - 2)
+    c = _case(oracle, EULER, 8, nx, dt)
+    ic = _euler_special_ic(oracle, nx, seed=nx + tpb + alg)
+    q = tpb // (2 * oracle.RADIUS[EULER] * oracle.SUBSTEPS[EULER])
+    for nsteps in (q, 2 * q + 3):
+        want = oracle.classic(c, ic, nsteps)
+        got, _ = _gpu(sw, solver, EULER, 8, alg, nx, tpb, dt, nsteps, ic)
+        _assert_same_or_both_nan(got, want, "euler alg %d nx %d tpb %d steps %d" % (alg, nx, tpb, nsteps))
+
+
 @pytest.mark.parametrize("problem", [HEAT, KS, EULER])
 def test_reference_time_mode_snapshots(sw, solver, oracle, problem):
     """SW_TIME_REFERENCE: snapshots at the reference's output times hold the
