@@ -651,8 +651,13 @@ int sw_closure_infer(sw_ctx *ctx, const float *theta, const float *u, float *del
     return SW_OK;
 }
 
-int sw_closure_step(sw_ctx *ctx, const sw_config *coarse, const float *theta, float *u, int32_t n_dom, int64_t n,
-                    int64_t n_steps, int32_t use_closure, sw_result *out) {
+}  // extern "C"
+
+namespace {
+// The coarse steps of sw_closure_step, enqueued on ctx's stream without
+// waiting for them (ctx->d_work is their second row buffer).
+int closure_enqueue(sw_ctx *ctx, const sw_config *coarse, const float *theta, float *u, int32_t n_dom, int64_t n,
+                    int64_t n_steps, int32_t use_closure) {
     int rc = closure_check(ctx, n_dom, n);
     if (rc) return rc;
     if (!coarse || !u || (use_closure && !theta)) return SW_ERR_ARG;
@@ -669,7 +674,6 @@ int sw_closure_step(sw_ctx *ctx, const sw_config *coarse, const float *theta, fl
     SW_CUDA(ctx, grow_dev(&ctx->d_work, &ctx->n_work, sizeof(float) * (size_t)n * n_dom));
     float *alt = static_cast<float *>(ctx->d_work), *cur = u;
     const int64_t tiles = n / cl::TOUT;
-    SW_CUDA(ctx, cudaEventRecord(ctx->k0, ctx->stream));
     const uint4 *w2p = nullptr;
     if (use_closure) {
         rc = stage_w2(ctx, theta, &w2p);
@@ -683,6 +687,19 @@ int sw_closure_step(sw_ctx *ctx, const sw_config *coarse, const float *theta, fl
     SW_CUDA(ctx, cudaGetLastError());
     if (cur != u) SW_CUDA(ctx, cudaMemcpyAsync(u, cur, sizeof(float) * (size_t)n * n_dom, cudaMemcpyDeviceToDevice,
                                                ctx->stream));
+    return SW_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int sw_closure_step(sw_ctx *ctx, const sw_config *coarse, const float *theta, float *u, int32_t n_dom, int64_t n,
+                    int64_t n_steps, int32_t use_closure, sw_result *out) {
+    if (!ctx) return SW_ERR_ARG;
+    SW_CUDA(ctx, cudaSetDevice(ctx->device));
+    SW_CUDA(ctx, cudaEventRecord(ctx->k0, ctx->stream));
+    const int rc = closure_enqueue(ctx, coarse, theta, u, n_dom, n, n_steps, use_closure);
+    if (rc) return rc;
     SW_CUDA(ctx, cudaEventRecord(ctx->k1, ctx->stream));
     SW_CUDA(ctx, cudaEventSynchronize(ctx->k1));
     if (out) {
@@ -690,7 +707,7 @@ int sw_closure_step(sw_ctx *ctx, const sw_config *coarse, const float *theta, fl
         cudaEventElapsedTime(&ms, ctx->k0, ctx->k1);
         std::memset(out, 0, sizeof(*out));
         out->n_steps = n_steps;
-        out->t_final = n_steps * c.dt;
+        out->t_final = n_steps * coarse->dt;
         out->kernel_ms = out->elapsed_ms = ms;
         out->launches = n_steps;
     }
@@ -795,11 +812,14 @@ int sw_closure_adaptive(sw_ctx *ctx, sw_ctx *judge, const sw_config *coarse, con
     if (idx.empty()) return fail(ctx, SW_ERR_ARG, "the judge's sample is empty");
     const int32_t m = (int32_t)idx.size();
     SW_CUDA(ctx, cudaSetDevice(ctx->device));
-    // run context scratch: the sample's coarse rows and reference (m x n floats each), indices, errors
-    const size_t fb = sizeof(float) * (size_t)m * n;
-    SW_CUDA(ctx, grow_dev(&ctx->d_judge, &ctx->n_judge, 2 * fb + 4 * sizeof(double) * m + sizeof(int32_t) * m + 64));
-    float *samp = static_cast<float *>(ctx->d_judge), *ref = samp + (size_t)m * n;
-    double *err = reinterpret_cast<double *>(ref + (size_t)m * n);  // [2][m]
+    // run context scratch: the sample's coarse rows for each variant and the reference (m x n
+    // floats each, at 256-byte boundaries), errors, indices
+    const size_t fb = sizeof(float) * (size_t)m * n, fbr = (fb + 255) & ~(size_t)255;
+    SW_CUDA(ctx, grow_dev(&ctx->d_judge, &ctx->n_judge, 3 * fbr + 4 * sizeof(double) * m + sizeof(int32_t) * m + 64));
+    char *scratch = static_cast<char *>(ctx->d_judge);
+    float *samp = reinterpret_cast<float *>(scratch), *samp2 = reinterpret_cast<float *>(scratch + fbr);
+    float *ref = reinterpret_cast<float *>(scratch + 2 * fbr);
+    double *err = reinterpret_cast<double *>(scratch + 3 * fbr);  // [2][m]
     int32_t *idx_d = reinterpret_cast<int32_t *>(err + 2 * m);
     SW_CUDA(ctx, grow_dev(&judge->d_judge, &judge->n_judge, sizeof(double) * (size_t)m * n_fine));
     double *shadow = static_cast<double *>(judge->d_judge);
@@ -836,18 +856,27 @@ int sw_closure_adaptive(sw_ctx *ctx, sw_ctx *judge, const sw_config *coarse, con
     int32_t nlog = 0;
     while (done < coarse_steps) {
         const int64_t k = std::min(segment, coarse_steps - done);
-        // the judge's segment first: its few launches run alone on the GPU
+        // The sample's runs first, enqueued: the first segment runs both variants on the
+        // sample, later ones the variant the ensemble does not run.  The judge's segment
+        // then runs on its own context beside them (a few small launches each), and the
+        // ensemble's run only after it, so that the judge is not held up behind the
+        // ensemble's thousands of blocks.
+        cl::k_gather_rows<float><<<m, 256, 0, s>>>(u_out, idx_d, n, samp);
+        SW_CUDA(ctx, cudaGetLastError());
+        if (pick < 0) {
+            SW_CUDA(ctx, cudaMemcpyAsync(samp2, samp, fb, cudaMemcpyDeviceToDevice, s));
+            if ((rc = closure_enqueue(ctx, coarse, theta, samp, m, n, k, 0))) return rc;
+            if ((rc = closure_enqueue(ctx, coarse, theta, samp2, m, n, k, 1))) return rc;
+        } else {
+            if ((rc = closure_enqueue(ctx, coarse, theta, samp, m, n, k, 1 - pick))) return rc;
+        }
         fc.n_steps = k * factor;
         if ((rc = sw_run_batch_device(judge, &fc, m, nx_s.data(), shadow, nullptr, nullptr))) return rc;
         if ((rc = sw_coarse_grain(judge, shadow, ref, (int64_t)m * n, factor))) return rc;
         int cur_slot, alt_slot;
-        if (pick < 0) {  // first segment: both variants on the sample, the better one on the ensemble
-            for (int v = 0; v < 2; ++v) {
-                cl::k_gather_rows<float><<<m, 256, 0, s>>>(u_out, idx_d, n, samp);
-                SW_CUDA(ctx, cudaGetLastError());
-                if ((rc = sw_closure_step(ctx, coarse, theta, samp, m, n, k, v, nullptr))) return rc;
-                if ((rc = rel(samp, nullptr, v))) return rc;
-            }
+        if (pick < 0) {  // first segment: the better variant on the sample runs the ensemble
+            if ((rc = rel(samp, nullptr, 0))) return rc;
+            if ((rc = rel(samp2, nullptr, 1))) return rc;
             SW_CUDA(ctx, cudaMemcpyAsync(h_err.data(), err, sizeof(double) * 2 * m, cudaMemcpyDeviceToHost, s));
             SW_CUDA(ctx, cudaStreamSynchronize(s));
             double m0, m1, x0, x1;
@@ -857,10 +886,7 @@ int sw_closure_adaptive(sw_ctx *ctx, sw_ctx *judge, const sw_config *coarse, con
             if ((rc = sw_closure_step(ctx, coarse, theta, u_out, n_dom, n, k, pick, nullptr))) return rc;
             cur_slot = pick;
             alt_slot = 1 - pick;
-        } else {  // the ensemble runs the pick, the other variant runs on the sample
-            cl::k_gather_rows<float><<<m, 256, 0, s>>>(u_out, idx_d, n, samp);
-            SW_CUDA(ctx, cudaGetLastError());
-            if ((rc = sw_closure_step(ctx, coarse, theta, samp, m, n, k, 1 - pick, nullptr))) return rc;
+        } else {  // the ensemble runs the pick (the other variant ran on the sample above)
             if ((rc = sw_closure_step(ctx, coarse, theta, u_out, n_dom, n, k, pick, nullptr))) return rc;
             if ((rc = rel(u_out, idx_d, 0))) return rc;
             if ((rc = rel(samp, nullptr, 1))) return rc;

@@ -468,9 +468,10 @@ cudaError_t launch_swept_batch(const void *vp, int mode, int phase, void *state,
     G *st = static_cast<G *>(state), *sl = static_cast<G *>(slots);
     if constexpr (P != SW_EULER) {
         // one cell per thread: G tiles of a domain per block, as the single-domain
-        // launcher groups them (KS four up to 1024 threads, Heat two up to 512)
+        // launcher groups them (KS four up to 1024 threads, Heat two up to 512),
+        // where blocks are plentiful
         constexpr int kMaxThreads = (P == SW_KS) ? 1024 : 512;
-        if (threads == W && !span4_launch<P, T>(W, threads)) {
+        if (threads == W && !span4_launch<P, T>(W, threads) && b.n_tiles >= kGroupMinTiles) {
             if (P == SW_KS && 4 * W <= kMaxThreads && b.group % 4 == 0)
                 return launch_swept_batch_group<P, T, 4>(p, mode, phase, st, sl, b, W, s);
             if (2 * W <= kMaxThreads && b.group % 2 == 0)
@@ -479,6 +480,10 @@ cudaError_t launch_swept_batch(const void *vp, int mode, int phase, void *state,
     }
     if (span4_launch<P, T>(W, threads))
         return launch_swept_batch_path<P, T, PATH_SPAN4>(p, mode, phase, st, sl, b, W, threads, s);
+    if constexpr (int_products<P, T>()) {  // few tiles: the FP64 products (PATH_CELL_FP)
+        if (few_tiles(b.n_tiles))
+            return launch_swept_batch_path<P, T, PATH_CELL_FP>(p, mode, phase, st, sl, b, W, threads, s);
+    }
     return launch_swept_batch_path<P, T, PATH_CELL>(p, mode, phase, st, sl, b, W, threads, s);
 }
 

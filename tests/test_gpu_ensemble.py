@@ -37,17 +37,18 @@ def test_ks_ensemble_bit_exact(sw, solver, oracle, prec, alg):
 @pytest.mark.parametrize("prec", [8, 4])
 def test_ensembles_of_grouped_tiles(sw, solver, oracle, prec):
     """Every domain a multiple of four tiles (KS) or two (Heat), one cell per
-    thread: the swept passes run G tiles of one domain per block, as the
-    single-domain kernel groups them (FP64 KS with bulk-copied slots).  Every
-    domain still equals the oracle run on it alone."""
+    thread, at least 1024 tiles in all: the swept passes run G tiles of one
+    domain per block, as the single-domain kernel groups them (FP64 KS with
+    bulk-copied slots).  Every domain still equals the oracle run on it alone."""
     dt = np.float64 if prec == 8 else np.float32
-    nx, ic = ens.make_ensemble(n_domains=24, lo=8, hi=11, seed=7, dtype=dt)
+    nx, ic = ens.make_ensemble(n_domains=96, lo=8, hi=11, seed=7, dtype=dt)
+    assert nx.sum() // 64 >= 1024
     cfg = sw.make_config(1, prec, alg=1, tpb=64, dt=0.005, time_mode=sw.TIME_STEPS, n_steps=52)
     out, res = solver.run_batch(cfg, nx, ic)
     assert res.n_steps == 52
     np.testing.assert_array_equal(out, _oracle_each(oracle, 1, prec, nx, ic, 0.005, 52))
     rng = np.random.default_rng(3)
-    nx = np.array([256, 128, 512, 128, 1024], dtype=np.int64)
+    nx = np.tile(np.array([256, 128, 512, 128, 1024], dtype=np.int64), 40)
     ic = (rng.standard_normal(int(nx.sum())) + 10.0).astype(dt)
     cfg = sw.make_config(0, prec, alg=1, tpb=64, dt=0.004, bc=sw.BC_PERIODIC, time_mode=sw.TIME_STEPS, n_steps=100)
     out, _ = solver.run_batch(cfg, nx, ic)
