@@ -14,7 +14,8 @@ the timing).
 by the library's own events and each checked bit for bit against our classic
 scheme on the same run:
   * swept_over_classic_2e22 -- Heat, KS and Euler at nx = 2^22, FP64 and FP32,
-    over a stated window of time steps;
+    over a stated window of time steps, each swept run at its fastest measured
+    tile width (perf.py's sweep);
   * cfg1 -- Heat FP64, periodic, nx = 4096, tpb = 128, Fourier number 0.1,
     20000 steps, with the error against the scheme's exact decaying mode;
   * cfg3 -- Euler/Sod FP64, nx = 2^22, tpb = 512, dt/dx = 0.1, a window of
@@ -278,7 +279,7 @@ def target_2e22(sw, solver) -> dict:
     rows = {}
     for key, problem, prec, tpb, steps, dt in (
             ("heat_f64", 0, 8, 1024, 4096, 0.004), ("heat_f32", 0, 4, 1024, 4096, 0.004),
-            ("ks_f64", 1, 8, 256, 2048, DT), ("ks_f32", 1, 4, 1024, 2048, DT),
+            ("ks_f64", 1, 8, 128, 2048, DT), ("ks_f32", 1, 4, 1024, 2048, DT),
             ("euler_f64", 2, 8, 512, 512, 0.1 / (big - 2)), ("euler_f32", 2, 4, 512, 512, 0.1 / (big - 2))):
         rows[key], _ = _pair(sw, solver, problem, prec, big, tpb, steps, dt)
     return rows
