@@ -794,6 +794,10 @@ int sw_closure_train(sw_ctx *ctx, float *theta, const float *inputs, const float
     return rc;
 }
 
+// Closure steps the ensemble runs in the first segment before the judge has
+// picked a variant: about the time the judge's first segment takes beside them.
+constexpr int64_t kSpeculativeSteps = 8;
+
 int sw_closure_adaptive(sw_ctx *ctx, sw_ctx *judge, const sw_config *coarse, const sw_config *fine,
                         const float *theta, const double *fine0, int32_t n_dom, int64_t n_fine, int32_t factor,
                         int64_t coarse_steps, int64_t segment, double tau, int32_t shadow_every,
@@ -813,13 +817,19 @@ int sw_closure_adaptive(sw_ctx *ctx, sw_ctx *judge, const sw_config *coarse, con
     const int32_t m = (int32_t)idx.size();
     SW_CUDA(ctx, cudaSetDevice(ctx->device));
     // run context scratch: the sample's coarse rows for each variant and the reference (m x n
-    // floats each, at 256-byte boundaries), errors, indices
+    // floats each), the ensemble's state kept at the start of the first segment, errors,
+    // indices (each at a 256-byte boundary)
     const size_t fb = sizeof(float) * (size_t)m * n, fbr = (fb + 255) & ~(size_t)255;
-    SW_CUDA(ctx, grow_dev(&ctx->d_judge, &ctx->n_judge, 3 * fbr + 4 * sizeof(double) * m + sizeof(int32_t) * m + 64));
+    const size_t ub = sizeof(float) * (size_t)n_dom * n, ubr = (ub + 255) & ~(size_t)255;
+    SW_CUDA(ctx, grow_dev(&ctx->d_judge, &ctx->n_judge,
+                          3 * fbr + ubr + 4 * sizeof(double) * m + sizeof(int32_t) * m + 64));
+    // the coarse runs' second row buffer, sized for the ensemble before any run is enqueued
+    SW_CUDA(ctx, grow_dev(&ctx->d_work, &ctx->n_work, ub));
     char *scratch = static_cast<char *>(ctx->d_judge);
     float *samp = reinterpret_cast<float *>(scratch), *samp2 = reinterpret_cast<float *>(scratch + fbr);
     float *ref = reinterpret_cast<float *>(scratch + 2 * fbr);
-    double *err = reinterpret_cast<double *>(scratch + 3 * fbr);  // [2][m]
+    float *u_kept = reinterpret_cast<float *>(scratch + 3 * fbr);
+    double *err = reinterpret_cast<double *>(scratch + 3 * fbr + ubr);  // [2][m]
     int32_t *idx_d = reinterpret_cast<int32_t *>(err + 2 * m);
     SW_CUDA(ctx, grow_dev(&judge->d_judge, &judge->n_judge, sizeof(double) * (size_t)m * n_fine));
     double *shadow = static_cast<double *>(judge->d_judge);
@@ -856,19 +866,27 @@ int sw_closure_adaptive(sw_ctx *ctx, sw_ctx *judge, const sw_config *coarse, con
     int32_t nlog = 0;
     while (done < coarse_steps) {
         const int64_t k = std::min(segment, coarse_steps - done);
-        // The sample's runs first, enqueued: the first segment runs both variants on the
-        // sample, later ones the variant the ensemble does not run.  The judge's segment
-        // then runs on its own context beside them (a few small launches each), and the
-        // ensemble's run only after it, so that the judge is not held up behind the
-        // ensemble's thousands of blocks.
+        // Enqueued first, in this order on the run's stream: the sample's runs (both
+        // variants in the first segment, later the variant the ensemble does not run),
+        // then the ensemble's run of the pick.  The judge's segment runs meanwhile on its
+        // own context, and the segment takes as long as the longer of the two.  The first
+        // segment's pick is not known yet: the ensemble starts the closure for the first
+        // kSpeculativeSteps steps (about the judge's time), its state at the segment's
+        // start kept, then continues it, or runs the plain step from the kept state
+        // should the sample pick that.  The results are those of running the pick alone.
         cl::k_gather_rows<float><<<m, 256, 0, s>>>(u_out, idx_d, n, samp);
         SW_CUDA(ctx, cudaGetLastError());
+        int64_t started = 0;  // closure steps the ensemble ran ahead of the first pick
         if (pick < 0) {
             SW_CUDA(ctx, cudaMemcpyAsync(samp2, samp, fb, cudaMemcpyDeviceToDevice, s));
             if ((rc = closure_enqueue(ctx, coarse, theta, samp, m, n, k, 0))) return rc;
             if ((rc = closure_enqueue(ctx, coarse, theta, samp2, m, n, k, 1))) return rc;
+            SW_CUDA(ctx, cudaMemcpyAsync(u_kept, u_out, ub, cudaMemcpyDeviceToDevice, s));
+            started = std::min(k, kSpeculativeSteps);
+            if ((rc = closure_enqueue(ctx, coarse, theta, u_out, n_dom, n, started, 1))) return rc;
         } else {
             if ((rc = closure_enqueue(ctx, coarse, theta, samp, m, n, k, 1 - pick))) return rc;
+            if ((rc = closure_enqueue(ctx, coarse, theta, u_out, n_dom, n, k, pick))) return rc;
         }
         fc.n_steps = k * factor;
         if ((rc = sw_run_batch_device(judge, &fc, m, nx_s.data(), shadow, nullptr, nullptr))) return rc;
@@ -883,11 +901,15 @@ int sw_closure_adaptive(sw_ctx *ctx, sw_ctx *judge, const sw_config *coarse, con
             stats(0, &m0, &x0);
             stats(1, &m1, &x1);
             pick = (m1 < m0) ? 1 : 0;
-            if ((rc = sw_closure_step(ctx, coarse, theta, u_out, n_dom, n, k, pick, nullptr))) return rc;
+            if (pick == 0) {  // the plain step, from the kept state
+                SW_CUDA(ctx, cudaMemcpyAsync(u_out, u_kept, ub, cudaMemcpyDeviceToDevice, s));
+                if ((rc = sw_closure_step(ctx, coarse, theta, u_out, n_dom, n, k, 0, nullptr))) return rc;
+            } else if (k > started) {  // the rest of the closure's segment
+                if ((rc = sw_closure_step(ctx, coarse, theta, u_out, n_dom, n, k - started, 1, nullptr))) return rc;
+            }
             cur_slot = pick;
             alt_slot = 1 - pick;
-        } else {  // the ensemble runs the pick (the other variant ran on the sample above)
-            if ((rc = sw_closure_step(ctx, coarse, theta, u_out, n_dom, n, k, pick, nullptr))) return rc;
+        } else {  // the ensemble ran the pick, the sample the other variant
             if ((rc = rel(u_out, idx_d, 0))) return rc;
             if ((rc = rel(samp, nullptr, 1))) return rc;
             SW_CUDA(ctx, cudaMemcpyAsync(h_err.data(), err, sizeof(double) * 2 * m, cudaMemcpyDeviceToHost, s));
